@@ -1,0 +1,181 @@
+/*
+ * kg_common.cu -- error reporting, parameter checks, derived constants and
+ * the nucleus seeding kernel.
+ */
+#include <math.h>
+#include <string.h>
+#include "kg_common.h"
+
+static thread_local char g_err[512];
+
+int kg_fail(int code, const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int kg_cuda_fail(cudaError_t e, const char* what)
+{
+    return kg_fail(e == cudaErrorMemoryAllocation ? KG_ERR_NOMEM : KG_ERR_CUDA, "%s: %s (%s)", what,
+                   cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+extern "C" const char* kg_last_error(void) { return g_err; }
+
+extern "C" const char* kg_version(void) { return "kobayashi-gb300 0.1 (sm_103a, FP64)"; }
+
+/* _parameterInit and the ctor's grid spacing (src/Kobayashi.cpp:61-63,76-84) */
+extern "C" int kg_params_default(kg_params* p, double dt)
+{
+    if (!p)
+        return kg_fail(KG_ERR_INVALID, "kg_params_default: null pointer");
+    p->dx = 0.03;
+    p->dy = 0.03;
+    p->dt = dt;
+    p->tau = 0.0003;
+    p->eps_bar = 0.010;
+    p->mu = 1.0;
+    p->K = 1.6;
+    p->delta = 0.05;
+    p->aniso = 6.0;
+    p->alpha = 0.9;
+    p->gamma = 10.0;
+    p->teq = 1.0;
+    p->theta0 = 0.0;
+    return KG_OK;
+}
+
+static bool finite_all(const kg_params* p)
+{
+    const double* v = &p->dx;
+    for (int i = 0; i < (int)(sizeof(kg_params) / sizeof(double)); i++)
+        if (!isfinite(v[i]))
+            return false;
+    return true;
+}
+
+extern "C" int kg_params_validate(const kg_params* p)
+{
+    if (!p)
+        return kg_fail(KG_ERR_INVALID, "params: null pointer");
+    if (!finite_all(p))
+        return kg_fail(KG_ERR_INVALID, "params: every field must be finite");
+    const double lo = 1e-12, hi = 1e12;
+    if (!(p->dx >= lo && p->dx <= hi && p->dy >= lo && p->dy <= hi))
+        return kg_fail(KG_ERR_INVALID, "params: dx, dy must lie in [1e-12, 1e12]");
+    if (!(p->dt > 0 && p->dt <= hi))
+        return kg_fail(KG_ERR_INVALID, "params: dt must be > 0");
+    if (!(p->tau >= lo && p->tau <= hi))
+        return kg_fail(KG_ERR_INVALID, "params: tau must lie in [1e-12, 1e12]");
+    if (!(p->eps_bar > 0))
+        return kg_fail(KG_ERR_INVALID, "params: eps_bar must be > 0");
+    if (!(p->aniso >= 1 && p->aniso <= 64 && p->aniso == floor(p->aniso)))
+        return kg_fail(KG_ERR_INVALID, "params: aniso (mode number j) must be an integer in [1, 64]");
+    if (!(fabs(p->theta0) <= 100.0))
+        return kg_fail(KG_ERR_INVALID, "params: |theta0| must be <= 100");
+    return KG_OK;
+}
+
+int kg_prepare(const kg_params* p, KgDev* d)
+{
+    int rc = kg_params_validate(p);
+    if (rc)
+        return rc;
+    memset(d, 0, sizeof *d);
+    d->dx = p->dx;
+    d->dy = p->dy;
+    d->dt = p->dt;
+    d->tau = p->tau;
+    d->eps_bar = p->eps_bar;
+    d->K = p->K;
+    d->delta = p->delta;
+    d->aniso = p->aniso;
+    d->alpha = p->alpha;
+    d->gamma = p->gamma;
+    d->teq = p->teq;
+    d->theta0 = p->theta0;
+    d->lap_den = 3.0 * p->dx * p->dx;
+    if (kg_cdiv_prepare(p->dx, &d->rdx_h, &d->rdx_l) || kg_cdiv_prepare(p->dy, &d->rdy_h, &d->rdy_l) ||
+        kg_cdiv_prepare(d->lap_den, &d->rlap_h, &d->rlap_l) || kg_cdiv_prepare(p->tau, &d->rtau_h, &d->rtau_l))
+        return kg_fail(KG_ERR_INVALID, "params: dx, dy, 3 dx^2 and tau must lie in [2^-100, 2^100]");
+    d->c_epsd = -p->eps_bar * p->aniso * p->delta;
+    d->a_pi = p->alpha / KG_PI;
+    /* memo for theta == 0: the same operations the kernel would do */
+    d->arg0 = p->aniso * (0.0 - p->theta0);
+    double s, c;
+    kg_sincos(d->arg0, &s, &c);
+    d->eps0 = p->eps_bar * (1.0 + p->delta * c);
+    d->epsd0 = d->c_epsd * s;
+    d->e2_0 = d->eps0 * d->eps0;
+    d->ee0 = d->eps0 * d->epsd0;
+    /* memo for T == 0 */
+    d->u0 = p->gamma * (p->teq - 0.0);
+    d->m0 = d->a_pi * kg_atan(d->u0);
+    return KG_OK;
+}
+
+__global__ void kg_seed_kernel(double* phi, double* t, double* theta, int nx, int ny, int n, const int* cx,
+                               const int* cy, const int* r)
+{
+    long long N = (long long)nx * ny;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N; c += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(c % nx), j = (int)(c / nx);
+        double v = 0.0;
+        for (int k = 0; k < n; k++) {
+            int di = (i - cx[k]) % nx;
+            if (di < 0)
+                di += nx;
+            if (di > nx / 2)
+                di -= nx;
+            int dj = (j - cy[k]) % ny;
+            if (dj < 0)
+                dj += ny;
+            if (dj > ny / 2)
+                dj -= ny;
+            if ((long long)di * di + (long long)dj * dj <= (long long)r[k] * r[k]) {
+                v = 1.0;
+                break;
+            }
+        }
+        phi[c] = v;
+        t[c] = 0.0;
+        theta[c] = 0.0;
+    }
+}
+
+int kg_seed_device(double* phi, double* t, double* theta, int nx, int ny, int n, const int* cx, const int* cy,
+                   const int* r, cudaStream_t s)
+{
+    if (n < 0 || (n > 0 && (!cx || !cy || !r)))
+        return kg_fail(KG_ERR_INVALID, "seed: bad disk list");
+    for (int k = 0; k < n; k++)
+        if (r[k] < 0)
+            return kg_fail(KG_ERR_INVALID, "seed: negative radius");
+    int* d = nullptr;
+    if (n > 0) {
+        KG_CUDA(cudaMalloc(&d, sizeof(int) * 3 * (size_t)n));
+        cudaError_t e = cudaMemcpyAsync(d, cx, sizeof(int) * n, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d + n, cy, sizeof(int) * n, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d + 2 * n, r, sizeof(int) * n, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) {
+            cudaFree(d);
+            return kg_cuda_fail(e, "seed: copy disks");
+        }
+    }
+    long long N = (long long)nx * ny;
+    int blocks = (int)((N + 255) / 256 < 152 * 16 ? (N + 255) / 256 : 152 * 16);
+    kg_seed_kernel<<<blocks, 256, 0, s>>>(phi, t, theta, nx, ny, n, d, d ? d + n : nullptr, d ? d + 2 * n : nullptr);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (d)
+        cudaFree(d);
+    if (e != cudaSuccess)
+        return kg_cuda_fail(e, "seed kernel");
+    return KG_OK;
+}

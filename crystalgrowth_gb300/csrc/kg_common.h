@@ -1,0 +1,31 @@
+/*
+ * kg_common.h -- host-side helpers shared by the library's translation units:
+ * error reporting, parameter validation and the preparation of the
+ * per-parameter-set constants (KgDev) that the kernels read.
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include "kobayashi_gpu.h"
+#include "kg_device.cuh"
+
+/* records a message for kg_last_error() and returns `code` */
+int kg_fail(int code, const char* fmt, ...);
+
+/* maps a CUDA error to KG_ERR_CUDA with a message naming `what` */
+int kg_cuda_fail(cudaError_t e, const char* what);
+
+#define KG_CUDA(call)                                              \
+    do {                                                           \
+        cudaError_t kg_e_ = (call);                                \
+        if (kg_e_ != cudaSuccess)                                  \
+            return kg_cuda_fail(kg_e_, #call);                     \
+    } while (0)
+
+/* fills the derived constants of one parameter set; returns KG_OK or KG_ERR_INVALID */
+int kg_prepare(const kg_params* p, KgDev* d);
+
+/* zero fields and seed disks on the device (kg_seed.cu) */
+int kg_seed_device(double* phi, double* t, double* theta, int nx, int ny, int n, const int* cx, const int* cy,
+                   const int* r, cudaStream_t s);

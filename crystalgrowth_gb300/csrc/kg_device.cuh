@@ -1,0 +1,228 @@
+/*
+ * kg_device.cuh -- the fused Kobayashi step on sm_103a.
+ *
+ * One explicit step of the reference (src/Kobayashi.cpp:125-221) in one pass
+ * over HBM: each CTA owns a strip of NT-2 columns and BH rows, and marches
+ * down its rows.  At row r it computes the stage-1 quantities that neighbours
+ * need (gradients, the persistent angle, eps, eps' and the products
+ * eps^2, eps eps' phi_x, eps eps' phi_y) for its NT columns (one halo column
+ * each side), keeps the vertical neighbours of those in registers and the
+ * horizontal ones in shared memory, and finishes stage 2 (the Laplacians, the
+ * divergence terms and the phi/T update) for row r-1.  Stage-1 work is
+ * therefore done once per cell plus 2/BH rows and 2/(NT-2) columns of halo;
+ * intermediate arrays never touch HBM (48 B/cell: phi, T, theta read and
+ * written once).
+ *
+ * The arithmetic reproduces the reference operation for operation in IEEE
+ * FP64 (this file is compiled with -fmad=false, so a*b+c is never fused
+ * unless written as kg_fma), with three exact shortcuts:
+ *   - divisions by dx, dy, 3 dx^2 and tau use kg_cdiv (same bits as a/b);
+ *   - eps, eps' for the angle value theta = 0 (every cell the front has not
+ *     reached) come from a table computed once on the host with the same
+ *     kg_sincos, keyed on the exact bits of the sine/cosine argument;
+ *   - m = alpha/pi atan(gamma (Teq - T)) for the far-field argument
+ *     gamma*Teq likewise.
+ * Comparisons use the bit patterns (integer pipe), never the FP64 pipe.
+ */
+#pragma once
+#include <stdint.h>
+#include "kg_math.h"
+
+/* Everything the kernel needs about one parameter set, prepared on the host. */
+struct KgDev {
+    double dx, dy, dt, tau, eps_bar, K, delta, aniso, alpha, gamma, teq, theta0;
+    double rdx_h, rdx_l, rdy_h, rdy_l, rlap_h, rlap_l, rtau_h, rtau_l; /* kg_cdiv reciprocals */
+    double lap_den;   /* (3 dx) dx, src/Kobayashi.cpp:146 */
+    double c_epsd;    /* ((-eps_bar) aniso) delta, src/Kobayashi.cpp:171 */
+    double a_pi;      /* alpha / PI_F, src/Kobayashi.cpp:206 */
+    double arg0;      /* aniso (0 - theta0): sin/cos argument of theta == 0 */
+    double eps0, epsd0, e2_0, ee0; /* eps, eps', eps^2, eps eps' at arg0 */
+    double u0, m0;    /* gamma (Teq - 0) and (alpha/pi) atan(u0) */
+};
+
+#define KG_ABS_MASK 0x7fffffffffffffffull
+#define KG_EPS_BITS 0x3e80000000000000ull /* FLT_EPSILON = 2^-23 as a double */
+#define KG_INF_BITS 0x7ff0000000000000ull
+
+/* x <= +eps && x >= -eps */
+__device__ __forceinline__ bool kg_small(uint64_t b) { return (b & KG_ABS_MASK) <= KG_EPS_BITS; }
+/* x > +eps */
+__device__ __forceinline__ bool kg_pos_big(uint64_t b) { return b > KG_EPS_BITS && b <= KG_INF_BITS; }
+/* x < -eps */
+__device__ __forceinline__ bool kg_neg_big(uint64_t b)
+{
+    return b > (0x8000000000000000ull | KG_EPS_BITS) && b <= 0xfff0000000000000ull;
+}
+
+/* Stage-1 quantities of one cell that its neighbours read in stage 2. */
+struct KgS1 {
+    double gx, gy, e2, a, b; /* phi_x, phi_y, eps^2, eps eps' phi_x, eps eps' phi_y */
+};
+
+/*
+ * Stage 1 for one cell (src/Kobayashi.cpp:139-140,154-171): gradients, the
+ * angle update (theta keeps its value in the FLT_EPSILON dead zone), eps, eps'.
+ * theta is updated in place.
+ */
+__device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, double pN, double pS, double& theta)
+{
+    KgS1 o;
+    double gx = kg_cdiv(pE - pW, P.dx, P.rdx_h, P.rdx_l);
+    double gy = kg_cdiv(pN - pS, P.dy, P.rdy_h, P.rdy_l);
+    uint64_t bx = kg_bits(gx), by = kg_bits(gy);
+    if (kg_small(bx)) {
+        if (kg_neg_big(by))
+            theta = -0.5 * KG_PI;
+        else if (kg_pos_big(by))
+            theta = 0.5 * KG_PI;
+    } else if (kg_pos_big(bx)) {
+        if (kg_neg_big(by))
+            theta = 2.0 * KG_PI + kg_atan(gy / gx);
+        else if (kg_pos_big(by))
+            theta = kg_atan(gy / gx);
+    } else if (kg_neg_big(bx)) {
+        theta = KG_PI + kg_atan(gy / gx);
+    }
+    double arg = P.aniso * (theta - P.theta0);
+    double e2, ee;
+    if (kg_bits(arg) == kg_bits(P.arg0)) {
+        e2 = P.e2_0;
+        ee = P.ee0;
+    } else {
+        double s, c;
+        kg_sincos(arg, &s, &c);
+        double eps = P.eps_bar * (1.0 + P.delta * c);
+        double epsd = P.c_epsd * s;
+        e2 = eps * eps;
+        ee = eps * epsd;
+    }
+    o.gx = gx;
+    o.gy = gy;
+    o.e2 = e2;
+    o.a = ee * gx;
+    o.b = ee * gy;
+    return o;
+}
+
+/* 9-point Laplacian in the reference's summation order (src/Kobayashi.cpp:142-151). */
+__device__ __forceinline__ double kg_lap(const KgDev& P, double c, double e, double w, double n, double s, double ne,
+                                         double sw, double nw, double se)
+{
+    double v = 2.0 * (e + w + n + s) + ne + sw + nw + se - 12.0 * c;
+    return kg_cdiv(v, P.lap_den, P.rlap_h, P.rlap_l);
+}
+
+/*
+ * Stage 2 for one cell (src/Kobayashi.cpp:190-215).  Neighbour stage-1 data:
+ * e2 at E/W/N/S, a = eps eps' phi_x at N/S, b = eps eps' phi_y at E/W.
+ */
+__device__ __forceinline__ void kg_stage2(const KgDev& P, double e2c, double gx, double gy, double e2E, double e2W,
+                                          double e2N, double e2S, double aN, double aS, double bE, double bW,
+                                          double lap_phi, double lap_t, double& phi, double& t)
+{
+    double gex = kg_cdiv(e2E - e2W, P.dx, P.rdx_h, P.rdx_l);
+    double gey = kg_cdiv(e2N - e2S, P.dy, P.rdy_h, P.rdy_l);
+    double term1 = kg_cdiv(aN - aS, P.dy, P.rdy_h, P.rdy_l);
+    double term2 = -kg_cdiv(bE - bW, P.dx, P.rdx_h, P.rdx_l);
+    double term3 = gex * gx + gey * gy;
+    double u = P.gamma * (P.teq - t);
+    double m = (kg_bits(u) == kg_bits(P.u0)) ? P.m0 : P.a_pi * kg_atan(u);
+    double old_phi = phi;
+    double old_t = t;
+    double rhs = term1 + term2 + e2c * lap_phi + term3 + old_phi * (1.0 - old_phi) * (old_phi - 0.5 + m);
+    double new_phi = old_phi + kg_cdiv(rhs * P.dt, P.tau, P.rtau_h, P.rtau_l);
+    t = old_t + lap_t * P.dt + P.K * (new_phi - old_phi);
+    phi = new_phi;
+}
+
+__device__ __forceinline__ int kg_wrap(int i, int n)
+{
+    int r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+/*
+ * The marching strip: one CTA of NT threads advances columns [i0, i0+NT-2)
+ * (clipped to nx) and rows [j0, j0+bh) (clipped to ny) of one grid by one
+ * step, reading (phi, T, theta) from `*_in` and writing `*_out`.
+ * Shared memory: phi ring 8 x (NT+2), T ring 4 x NT, e2/b ring 2 x 2 x NT.
+ */
+template <int NT>
+struct KgSmem {
+    double phi[8][NT + 2];
+    double t[4][NT];
+    double e2[2][NT];
+    double b[2][NT];
+};
+
+template <int NT>
+__device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const double* __restrict__ phi_in,
+                                         const double* __restrict__ t_in, const double* __restrict__ th_in,
+                                         double* __restrict__ phi_out, double* __restrict__ t_out,
+                                         double* __restrict__ th_out, int i0, int j0, int bh, KgSmem<NT>& sm)
+{
+    const int L = threadIdx.x;
+    const int jend = min(j0 + bh, ny);
+    /* columns: phi smem index k <-> column i0-2+k; lane L <-> column i0-1+L */
+    const int colA = kg_wrap(i0 - 2 + L, nx);
+    const int colB = (L < 2) ? kg_wrap(i0 - 2 + NT + L, nx) : 0;
+    const int col = kg_wrap(i0 - 1 + L, nx);
+    const bool out_lane = (L >= 1) && (L <= NT - 2) && (i0 - 1 + L < nx);
+
+    auto load_phi_row = [&](int q) {
+        const double* row = phi_in + (size_t)kg_wrap(q, ny) * nx;
+        sm.phi[q & 7][L] = row[colA];
+        if (L < 2)
+            sm.phi[q & 7][NT + L] = row[colB];
+    };
+    /* rows j0-2 and j0-1 of phi before the march */
+    load_phi_row(j0 - 2);
+    load_phi_row(j0 - 1);
+
+    /* registers: stage-1 results of this lane's column for rows r-2, r-1, r */
+    double e2_m2 = 0, a_m2 = 0;
+    double e2_m1 = 0, a_m1 = 0, gx_m1 = 0, gy_m1 = 0;
+    for (int r = j0 - 1; r <= jend; r++) {
+        /* loads: phi row r+1, T row r, theta of this lane at row r */
+        load_phi_row(r + 1);
+        const size_t roff = (size_t)kg_wrap(r, ny) * nx;
+        sm.t[r & 3][L] = t_in[roff + col];
+        double theta = th_in[roff + col];
+        __syncthreads();
+
+        /* stage 1 at row r for all NT lanes */
+        KgS1 s1 = kg_stage1(P, sm.phi[r & 7][L + 2], sm.phi[r & 7][L], sm.phi[(r + 1) & 7][L + 1],
+                            sm.phi[(r - 1) & 7][L + 1], theta);
+        sm.e2[r & 1][L] = s1.e2;
+        sm.b[r & 1][L] = s1.b;
+        if (out_lane && r >= j0 && r < jend)
+            th_out[roff + col] = theta;
+
+        /* stage 2 at row s = r-1 for the output lanes */
+        const int s = r - 1;
+        if (out_lane && s >= j0) {
+            const int sm1 = (s - 1) & 7, s0 = s & 7, sp1 = (s + 1) & 7;
+            const int k = L + 1;
+            double lap_phi = kg_lap(P, sm.phi[s0][k], sm.phi[s0][k + 1], sm.phi[s0][k - 1], sm.phi[sp1][k],
+                                    sm.phi[sm1][k], sm.phi[sp1][k + 1], sm.phi[sm1][k - 1], sm.phi[sp1][k - 1],
+                                    sm.phi[sm1][k + 1]);
+            const int t0 = s & 3, tm = (s - 1) & 3, tp = (s + 1) & 3;
+            double lap_t = kg_lap(P, sm.t[t0][L], sm.t[t0][L + 1], sm.t[t0][L - 1], sm.t[tp][L], sm.t[tm][L],
+                                  sm.t[tp][L + 1], sm.t[tm][L - 1], sm.t[tp][L - 1], sm.t[tm][L + 1]);
+            double phi = sm.phi[s0][k];
+            double t = sm.t[t0][L];
+            kg_stage2(P, e2_m1, gx_m1, gy_m1, sm.e2[s & 1][L + 1], sm.e2[s & 1][L - 1], s1.e2, e2_m2, s1.a, a_m2,
+                      sm.b[s & 1][L + 1], sm.b[s & 1][L - 1], lap_phi, lap_t, phi, t);
+            const size_t soff = (size_t)kg_wrap(s, ny) * nx;
+            phi_out[soff + col] = phi;
+            t_out[soff + col] = t;
+        }
+        /* roll the vertical window */
+        e2_m2 = e2_m1;
+        a_m2 = a_m1;
+        e2_m1 = s1.e2;
+        a_m1 = s1.a;
+        gx_m1 = s1.gx;
+        gy_m1 = s1.gy;
+    }
+}

@@ -1,0 +1,265 @@
+/*
+ * kg_math.h -- the elementary functions of the Kobayashi step, written once
+ * for host and device.
+ *
+ * The reference (src/Kobayashi.cpp:162,164,167,170,171,206) calls the C
+ * library's atan, cos and sin.  The C library's double versions are not
+ * correctly rounded and differ between libm builds (and between x86-64 and
+ * aarch64), so a GPU kernel cannot reproduce them bit for bit.  This header
+ * defines the functions instead: every result is a fixed sequence of IEEE-754
+ * double operations (add, mul, explicit fma, one correctly rounded FP32
+ * reciprocal as a seed), so the CUDA kernels and the CPU oracle, which both
+ * include this file, compute identical bits on any IEEE-754 machine as long as
+ * the compiler does not contract a*b+c (host: -ffp-contract=off; device:
+ * -fmad=false).
+ *
+ * Methods (published; coefficients in kg_math_tables.h come from
+ * gen_kg_math_tables.py, which evaluates the mathematics in 320-bit precision):
+ *   kg_atan   table-driven Taylor expansion around c_k = k/128 (Gal's
+ *             accurate-tables method), argument reduction atan(x) =
+ *             pi/2 - atan(1/x) for |x| > 1 with a Newton-refined reciprocal.
+ *   kg_sincos Cody-Waite additive reduction by pi/128 (three-part), then
+ *             sin(nh + r) = S_n cos r + C_n sin r with tabulated S_n, C_n.
+ *   kg_cdiv   division by a divisor b fixed for a whole run: Markstein's
+ *             correction q = q0 + (a - b q0) * RN(1/b) applied to a faithful
+ *             quotient q0 = a * (1/b as a hi+lo pair); returns RN(a/b), i.e.
+ *             the same bits as the IEEE division a/b (Markstein 1990; the
+ *             hi+lo reciprocal makes q0 faithful).  Operands outside
+ *             [2^-900, 2^900] in magnitude fall back to a/b.
+ *
+ * Accuracy: kg_atan and kg_sincos are faithful (error < 1 ulp) on the
+ * documented domains; kg_sincos requires |x| < 4096 and returns NaN outside.
+ *
+ * This header is C99 and CUDA C++ at the same time (the oracle is plain C).
+ */
+#ifndef KG_MATH_H
+#define KG_MATH_H
+
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+#include "kg_math_tables.h"
+
+#if defined(__CUDACC__)
+#define KG_HD static __host__ __device__ __forceinline__
+#else
+#define KG_HD static inline
+#endif
+
+#if defined(__CUDACC__)
+__device__ static const double kg_atan_tab_dev[(KG_ATAN_N + 1) * KG_ATAN_STRIDE] = KG_ATAN_TAB_DATA;
+__device__ static const double kg_sc_tab_dev[KG_SC_N * 4] = KG_SC_TAB_DATA;
+#endif
+static const double kg_atan_tab_host[(KG_ATAN_N + 1) * KG_ATAN_STRIDE] = KG_ATAN_TAB_DATA;
+static const double kg_sc_tab_host[KG_SC_N * 4] = KG_SC_TAB_DATA;
+
+KG_HD double kg_tab_atan(int i)
+{
+#if defined(__CUDA_ARCH__)
+    return __ldg(&kg_atan_tab_dev[i]);
+#else
+    return kg_atan_tab_host[i];
+#endif
+}
+
+KG_HD double kg_tab_sc(int i)
+{
+#if defined(__CUDA_ARCH__)
+    return __ldg(&kg_sc_tab_dev[i]);
+#else
+    return kg_sc_tab_host[i];
+#endif
+}
+
+KG_HD uint64_t kg_bits(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t u;
+    memcpy(&u, &x, sizeof u);
+    return u;
+#endif
+}
+
+KG_HD double kg_from_bits(uint64_t u)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)u);
+#else
+    double x;
+    memcpy(&x, &u, sizeof x);
+    return x;
+#endif
+}
+
+/* fused multiply-add with a single rounding on both sides */
+KG_HD double kg_fma(double a, double b, double c)
+{
+#if defined(__CUDA_ARCH__)
+    return __fma_rn(a, b, c);
+#else
+    return fma(a, b, c);
+#endif
+}
+
+/* correctly rounded FP32 reciprocal of a correctly rounded FP32 conversion */
+KG_HD double kg_rcp_seed(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return (double)__frcp_rn(__double2float_rn(x));
+#else
+    float xf = (float)x;
+    float r = 1.0f / xf;
+    return (double)r;
+#endif
+}
+
+/* round-to-nearest-even of an FP32 value to int (|v| < 2^23) */
+KG_HD int kg_rint_f(float v)
+{
+#if defined(__CUDA_ARCH__)
+    return __float2int_rn(v);
+#else
+    return (int)lrintf(v);
+#endif
+}
+
+/*
+ * atan(x), faithful for every double (NaN propagates).
+ *   |x| <= 1 : t = |x|
+ *   |x| > 1  : t + tlo = 1/|x| (Newton-refined FP32 seed), result pi/2 - atan(t)
+ *   k = nearest node of t on the grid k/128, d = t - k/128 (exact), |d| <= 1/256
+ *   atan(t) = A_k + d * P_k(d), P_k the degree-6 Horner tail of the Taylor series
+ */
+KG_HD double kg_atan(double x)
+{
+    /* comparisons on the bit pattern: exact, and off the FP64 pipe on the GPU */
+    uint64_t ux = kg_bits(x);
+    uint64_t ua = ux & 0x7fffffffffffffffull;
+    double ax = kg_from_bits(ua);
+    if (ua > 0x43f0000000000000ull) {          /* |x| > 2^64, inf or NaN */
+        if (ua > 0x7ff0000000000000ull)
+            return x + x;
+        return (ux >> 63) ? -KG_PIO2_HI : KG_PIO2_HI;
+    }
+    double t, tlo = 0.0;
+    int inv = ua > 0x3ff0000000000000ull;      /* |x| > 1 */
+    if (inv) {
+        double y0 = kg_rcp_seed(ax);
+        double e0 = kg_fma(-ax, y0, 1.0);
+        double y1 = kg_fma(y0, e0, y0);
+        double e1 = kg_fma(-ax, y1, 1.0);
+        t = y1;
+        tlo = y1 * e1;
+    } else {
+        t = ax;
+    }
+#if defined(__CUDA_ARCH__)
+    int k = (int)__fadd_rn(__fmul_rn(__double2float_rn(t), (float)KG_ATAN_N), 0.5f);
+#else
+    float tf = (float)t;
+    float tk = tf * (float)KG_ATAN_N;
+    int k = (int)(tk + 0.5f);
+#endif
+    int b = k * KG_ATAN_STRIDE;
+    double d = t - kg_tab_atan(b + 0);
+    if (inv)
+        d = d + tlo;
+    double p = kg_tab_atan(b + 11);
+    p = kg_fma(d, p, kg_tab_atan(b + 10));
+    p = kg_fma(d, p, kg_tab_atan(b + 9));
+    p = kg_fma(d, p, kg_tab_atan(b + 8));
+    p = kg_fma(d, p, kg_tab_atan(b + 7));
+    p = kg_fma(d, p, kg_tab_atan(b + 6));
+    p = kg_fma(d, p, kg_tab_atan(b + 5));
+    double r;
+    if (inv)
+        r = kg_tab_atan(b + 3) + kg_fma(-d, p, kg_tab_atan(b + 4));
+    else
+        r = kg_tab_atan(b + 1) + kg_fma(d, p, kg_tab_atan(b + 2));
+    return (ux >> 63) ? -r : r;
+}
+
+/*
+ * sin(x) and cos(x) for |x| < 4096 (NaN outside).
+ *   n = nearest integer to x*128/pi (picked in FP32; any nearby n is fine),
+ *   r = x - n*H1 - n*H2 - n*H3 (three-part Cody-Waite; the first fma is exact), |r| <~ pi/256,
+ *   sin x = S_n (1 - pc) + C_n (r + r*ps),  cos x = C_n (1 - pc) - S_n (r + r*ps)
+ * with ps = sin(r)/r - 1 and pc = 1 - cos(r) as short Taylor polynomials in r^2.
+ */
+KG_HD void kg_sincos(double x, double* s_out, double* c_out)
+{
+    if ((kg_bits(x) & 0x7fffffffffffffffull) >= 0x40b0000000000000ull) { /* |x| >= 4096, inf, NaN */
+        double nan_ = kg_from_bits(0x7ff8000000000000ull);
+        *s_out = nan_;
+        *c_out = nan_;
+        return;
+    }
+#if defined(__CUDA_ARCH__)
+    int n = kg_rint_f(__fmul_rn(__double2float_rn(x), KG_SC_INV_H_F));
+#else
+    float xf = (float)x;
+    float xn = xf * KG_SC_INV_H_F;
+    int n = kg_rint_f(xn);
+#endif
+    double nd = (double)n;
+    double r = kg_fma(-nd, KG_SC_H1, x);
+    r = kg_fma(-nd, KG_SC_H2, r);
+    r = kg_fma(-nd, KG_SC_H3, r);
+    int b = (n & (KG_SC_N - 1)) * 4;
+    double sh = kg_tab_sc(b + 0), sl = kg_tab_sc(b + 1);
+    double ch = kg_tab_sc(b + 2), cl = kg_tab_sc(b + 3);
+    double z = r * r;
+    double ps = kg_fma(z, KG_S7, KG_S5);
+    ps = kg_fma(z, ps, KG_S3);
+    ps = z * ps;
+    double pc = kg_fma(z, KG_C6, KG_C4);
+    pc = kg_fma(z, pc, KG_C2);
+    pc = z * pc;
+    double rp = r * ps;
+    double st = kg_fma(ch, rp, sl);
+    st = kg_fma(-sh, pc, st);
+    st = kg_fma(cl, r, st);
+    st = kg_fma(ch, r, st);
+    double ct = kg_fma(-sh, rp, cl);
+    ct = kg_fma(-ch, pc, ct);
+    ct = kg_fma(-sl, r, ct);
+    ct = kg_fma(-sh, r, ct);
+    *s_out = sh + st;
+    *c_out = ch + ct;
+}
+
+/*
+ * Reciprocal pair for kg_cdiv: yh = RN(1/b), yl = RN((1 - b*yh)/b).
+ * Valid for 2^-100 <= b <= 2^100; returns 0 on success, -1 otherwise.
+ */
+KG_HD int kg_cdiv_prepare(double b, double* yh, double* yl)
+{
+    if (!(b >= 0x1p-100 && b <= 0x1p100))
+        return -1;
+    double h = 1.0 / b;
+    double e = kg_fma(-b, h, 1.0); /* exact: 1 - b*h fits in 53 bits */
+    *yh = h;
+    *yl = e / b;
+    return 0;
+}
+
+/*
+ * a / b with the bits of the IEEE division, for a divisor b prepared by
+ * kg_cdiv_prepare.  4 double operations instead of the ~8 of a general
+ * division.  Zero, tiny (< 2^-900), huge (>= 2^900), infinite and NaN
+ * dividends take the IEEE division itself.
+ */
+KG_HD double kg_cdiv(double a, double b, double yh, double yl)
+{
+    uint64_t ea = (kg_bits(a) >> 52) & 0x7ff;
+    if (ea - (1023u - 900u) < 1800u) {
+        double q0 = kg_fma(a, yh, a * yl);
+        double r = kg_fma(-q0, b, a);
+        return kg_fma(r, yh, q0);
+    }
+    return a / b;
+}
+
+#endif /* KG_MATH_H */

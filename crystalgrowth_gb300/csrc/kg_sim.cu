@@ -1,0 +1,342 @@
+/*
+ * kg_sim.cu -- the single-grid simulation handle (kg_sim) and its step kernel.
+ *
+ * State lives in HBM as two ping-pong copies of (phi, T, theta), nx*ny FP64
+ * each, row-major like the reference's std::vector fields
+ * (src/Kobayashi.h:107-115).  kg_step launches one fused kernel per time step
+ * (kg_device.cuh) and replays them as CUDA graphs of `chunk` steps.
+ */
+#include <string.h>
+#include <new>
+#include "kg_common.h"
+
+#ifndef KG_NT
+#define KG_NT 128 /* threads (= columns incl. 2 halo) per strip */
+#endif
+#ifndef KG_BH
+#define KG_BH 64  /* rows per strip */
+#endif
+
+template <int NT>
+__global__ void __launch_bounds__(NT) kg_step_kernel(const __grid_constant__ KgDev P, int nx, int ny, int bh,
+                                                     const double* __restrict__ phi_in, const double* __restrict__ t_in,
+                                                     const double* __restrict__ th_in, double* __restrict__ phi_out,
+                                                     double* __restrict__ t_out, double* __restrict__ th_out)
+{
+    __shared__ KgSmem<NT> sm;
+    kg_strip<NT>(P, nx, ny, phi_in, t_in, th_in, phi_out, t_out, th_out, blockIdx.x * (NT - 2), blockIdx.y * bh, bh,
+                 sm);
+}
+
+struct kg_sim {
+    int nx = 0, ny = 0;
+    kg_params p{};
+    KgDev dev{};
+    double* buf[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    int cur = 0;
+    cudaStream_t stream = nullptr;
+    long long steps = 0, frames = 0;
+    int chunk = 100;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int bh = KG_BH;
+};
+
+static void drop_graphs(kg_sim* h)
+{
+    for (int k = 0; k < 2; k++)
+        if (h->graph[k]) {
+            cudaGraphExecDestroy(h->graph[k]);
+            h->graph[k] = nullptr;
+        }
+}
+
+static int launch_step(kg_sim* h, int from)
+{
+    const int NT = KG_NT;
+    dim3 grid((h->nx + NT - 3) / (NT - 2), (h->ny + h->bh - 1) / h->bh);
+    double* const* a = h->buf[from];
+    double* const* b = h->buf[from ^ 1];
+    kg_step_kernel<NT><<<grid, NT, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1], b[2]);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return kg_cuda_fail(e, "kg_step_kernel launch");
+    return KG_OK;
+}
+
+/* a graph of h->chunk consecutive steps starting from ping-pong copy `from` */
+static int build_graph(kg_sim* h, int from)
+{
+    cudaGraph_t g = nullptr;
+    KG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = KG_OK;
+    int c = from;
+    for (int s = 0; s < h->chunk && rc == KG_OK; s++) {
+        rc = launch_step(h, c);
+        c ^= 1;
+    }
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (rc != KG_OK) {
+        if (g)
+            cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess)
+        return kg_cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&h->graph[from], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        h->graph[from] = nullptr;
+        return kg_cuda_fail(e, "cudaGraphInstantiate");
+    }
+    return KG_OK;
+}
+
+static int check(const kg_sim* h)
+{
+    if (!h)
+        return kg_fail(KG_ERR_INVALID, "null kg_sim handle");
+    return KG_OK;
+}
+
+extern "C" int kg_destroy(kg_sim* h)
+{
+    if (!h)
+        return KG_OK;
+    drop_graphs(h);
+    if (h->stream)
+        cudaStreamSynchronize(h->stream);
+    for (int k = 0; k < 2; k++)
+        for (int f = 0; f < 3; f++)
+            if (h->buf[k][f])
+                cudaFree(h->buf[k][f]);
+    if (h->stream)
+        cudaStreamDestroy(h->stream);
+    delete h;
+    return KG_OK;
+}
+
+extern "C" int kg_seed_disks(kg_sim* h, int n, const int* cx, const int* cy, const int* r)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    double* const* a = h->buf[h->cur];
+    rc = kg_seed_device(a[0], a[1], a[2], h->nx, h->ny, n, cx, cy, r, h->stream);
+    if (rc)
+        return rc;
+    h->steps = 0;
+    h->frames = 0;
+    return KG_OK;
+}
+
+extern "C" int kg_reset(kg_sim* h)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    /* _createNucleus(nx/2, ny/2): the centre and its four neighbours (src/Kobayashi.cpp:113-123) */
+    int cx = h->nx / 2, cy = h->ny / 2, r = 1;
+    return kg_seed_disks(h, 1, &cx, &cy, &r);
+}
+
+extern "C" int kg_create(int nx, int ny, const kg_params* p, kg_sim** out)
+{
+    if (!out)
+        return kg_fail(KG_ERR_INVALID, "kg_create: null output pointer");
+    *out = nullptr;
+    if (nx < 1 || ny < 1 || (long long)nx * ny > (1ll << 34))
+        return kg_fail(KG_ERR_INVALID, "kg_create: grid %d x %d out of range", nx, ny);
+    KgDev dev;
+    int rc = kg_prepare(p, &dev);
+    if (rc)
+        return rc;
+    kg_sim* h = new (std::nothrow) kg_sim();
+    if (!h)
+        return kg_fail(KG_ERR_NOMEM, "kg_create: host allocation");
+    h->nx = nx;
+    h->ny = ny;
+    h->p = *p;
+    h->dev = dev;
+    if (ny < h->bh)
+        h->bh = ny;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    size_t bytes = sizeof(double) * (size_t)nx * ny;
+    for (int k = 0; k < 2 && e == cudaSuccess; k++)
+        for (int f = 0; f < 3 && e == cudaSuccess; f++)
+            e = cudaMalloc(&h->buf[k][f], bytes);
+    if (e != cudaSuccess) {
+        rc = kg_cuda_fail(e, "kg_create: device allocation");
+        kg_destroy(h);
+        return rc;
+    }
+    rc = kg_reset(h);
+    if (rc) {
+        kg_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return KG_OK;
+}
+
+extern "C" int kg_set_params(kg_sim* h, const kg_params* p)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    KgDev dev;
+    rc = kg_prepare(p, &dev);
+    if (rc)
+        return rc;
+    h->p = *p;
+    h->dev = dev;
+    drop_graphs(h);
+    return KG_OK;
+}
+
+extern "C" int kg_get_params(const kg_sim* h, kg_params* p)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (!p)
+        return kg_fail(KG_ERR_INVALID, "kg_get_params: null pointer");
+    *p = h->p;
+    return KG_OK;
+}
+
+extern "C" int kg_set_graph_chunk(kg_sim* h, int chunk)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (chunk < 0 || chunk > 100000)
+        return kg_fail(KG_ERR_INVALID, "kg_set_graph_chunk: chunk %d out of range", chunk);
+    h->chunk = chunk;
+    drop_graphs(h);
+    return KG_OK;
+}
+
+extern "C" int kg_step(kg_sim* h, long long nsteps)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (nsteps < 0)
+        return kg_fail(KG_ERR_INVALID, "kg_step: negative step count");
+    while (h->chunk > 0 && nsteps >= h->chunk) {
+        if (!h->graph[h->cur]) {
+            rc = build_graph(h, h->cur);
+            if (rc)
+                return rc;
+        }
+        cudaError_t e = cudaGraphLaunch(h->graph[h->cur], h->stream);
+        if (e != cudaSuccess)
+            return kg_cuda_fail(e, "cudaGraphLaunch");
+        h->cur ^= (h->chunk & 1);
+        h->steps += h->chunk;
+        nsteps -= h->chunk;
+    }
+    for (; nsteps > 0; nsteps--) {
+        rc = launch_step(h, h->cur);
+        if (rc)
+            return rc;
+        h->cur ^= 1;
+        h->steps++;
+    }
+    return KG_OK;
+}
+
+extern "C" int kg_update(kg_sim* h)
+{
+    int rc = kg_step(h, 10);
+    if (rc)
+        return rc;
+    h->frames++;
+    return KG_OK;
+}
+
+extern "C" int kg_sync(kg_sim* h)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    KG_CUDA(cudaStreamSynchronize(h->stream));
+    return KG_OK;
+}
+
+extern "C" int kg_get_fields(kg_sim* h, double* phi, double* T, double* theta)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    size_t bytes = sizeof(double) * (size_t)h->nx * h->ny;
+    double* dst[3] = {phi, T, theta};
+    for (int f = 0; f < 3; f++)
+        if (dst[f])
+            KG_CUDA(cudaMemcpyAsync(dst[f], h->buf[h->cur][f], bytes, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(cudaStreamSynchronize(h->stream));
+    return KG_OK;
+}
+
+extern "C" int kg_set_fields(kg_sim* h, const double* phi, const double* T, const double* theta)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    size_t bytes = sizeof(double) * (size_t)h->nx * h->ny;
+    const double* src[3] = {phi, T, theta};
+    for (int f = 0; f < 3; f++)
+        if (src[f])
+            KG_CUDA(cudaMemcpyAsync(h->buf[h->cur][f], src[f], bytes, cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(cudaStreamSynchronize(h->stream));
+    return KG_OK;
+}
+
+extern "C" int kg_get_size(const kg_sim* h, int* nx, int* ny)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (nx)
+        *nx = h->nx;
+    if (ny)
+        *ny = h->ny;
+    return KG_OK;
+}
+
+extern "C" int kg_get_counters(const kg_sim* h, long long* steps, long long* frames)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (steps)
+        *steps = h->steps;
+    if (frames)
+        *frames = h->frames;
+    return KG_OK;
+}
+
+extern "C" int kg_device_fields(kg_sim* h, double** phi, double** T, double** theta)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (phi)
+        *phi = h->buf[h->cur][0];
+    if (T)
+        *T = h->buf[h->cur][1];
+    if (theta)
+        *theta = h->buf[h->cur][2];
+    return KG_OK;
+}
+
+extern "C" int kg_get_stream(kg_sim* h, void** stream)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (!stream)
+        return kg_fail(KG_ERR_INVALID, "kg_get_stream: null pointer");
+    *stream = (void*)h->stream;
+    return KG_OK;
+}

@@ -1,0 +1,127 @@
+/*
+ * kobayashi_gpu.h -- C ABI of the GB300 Kobayashi phase-field library
+ * (libkobayashi_gpu.so).
+ *
+ * This is the drop-in boundary for the simulation core of jklae/CrystalGrowth.
+ * The reference has no FFI: its boundary is the C++ class Kobayashi behind
+ * DXViewer's ISimulation interface (src/Kobayashi.h:32-68).  Each entry point
+ * below names the reference member it replaces.  include/kobayashi.hpp wraps
+ * this ABI in a C++ class with the reference's method names.
+ *
+ * Conventions
+ *   - Every function returns an int status: KG_OK (0) or a negative KG_ERR_*;
+ *     nothing aborts or throws.  kg_last_error() returns a message for the
+ *     calling thread's most recent failure.
+ *   - Plain pointers and sizes only.  Host buffers belong to the caller; device
+ *     memory belongs to the library.  Fields are row-major FP64, index
+ *     i + nx*j (src/Kobayashi.h:91).
+ *   - One handle = one CUDA stream on the current device; a handle is not
+ *     thread-safe (the reference is single-threaded too).  kg_step and
+ *     kg_update only enqueue work; calls that return host data synchronise.
+ *   - Arithmetic is IEEE FP64 with the reference's operation order; atan, sin
+ *     and cos are the library's own faithful implementations (kg_math.h), the
+ *     same on the CPU oracle and the GPU.
+ */
+#ifndef KOBAYASHI_GPU_H
+#define KOBAYASHI_GPU_H
+
+#if defined(__GNUC__)
+#define KG_API __attribute__((visibility("default")))
+#else
+#define KG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KG_OK 0
+#define KG_ERR_INVALID (-1)  /* bad argument (null pointer, size, parameter out of range) */
+#define KG_ERR_CUDA (-2)     /* CUDA runtime error; see kg_last_error() */
+#define KG_ERR_NOMEM (-3)    /* device or host allocation failed */
+#define KG_ERR_TIMEOUT (-4)  /* a bounded device-side wait ran out (batched kernel) */
+
+/* Model parameters.  Field meaning and defaults follow the reference's members
+ * (src/Kobayashi.h:94-105, defaults src/Kobayashi.cpp:61-63,76-84).  theta0 (the
+ * preferred growth angle) is an extension: eps = eps_bar (1 + delta cos(aniso
+ * (theta - theta0))); theta0 = 0 reproduces the reference bit for bit. */
+typedef struct kg_params {
+    double dx, dy, dt;
+    double tau, eps_bar, mu, K, delta, aniso, alpha, gamma, teq;
+    double theta0;
+} kg_params;
+
+typedef struct kg_sim kg_sim;
+
+/* Reference defaults: _parameterInit + the ctor's _dx/_dy/_dt
+ * (src/Kobayashi.cpp:61-63,76-84); mu is kept although the step never reads it. */
+KG_API int kg_params_default(kg_params* p, double dt);
+
+/* Checks a parameter set: finite values, dx, dy, dt, tau > 0 (and within
+ * [2^-100, 2^100]), eps_bar > 0, |theta0| <= 100, aniso an integer-valued
+ * value in [1, 64]. */
+KG_API int kg_params_validate(const kg_params* p);
+
+/* Kobayashi(int x, int y, float timeStep) + _vectorInit (src/Kobayashi.cpp:7-67,
+ * 98-123): allocates the grid on the current device, zeroes phi, T and theta
+ * and seeds the reference's 5-cell nucleus at (nx/2, ny/2).  nx, ny >= 1
+ * (the nucleus wraps periodically; for nx, ny >= 3 it is the reference's). */
+KG_API int kg_create(int nx, int ny, const kg_params* p, kg_sim** out);
+
+/* ~Kobayashi (src/Kobayashi.cpp:69-71) */
+KG_API int kg_destroy(kg_sim* h);
+
+/* iResetSimulationState (src/Kobayashi.cpp:241-249) without the viewer calls:
+ * _vectorInit again, step and frame counters back to 0; parameters persist. */
+KG_API int kg_reset(kg_sim* h);
+
+/* Generalised nucleus: zero all fields and set phi = 1 on n disks
+ * {(i,j): di^2 + dj^2 <= r^2} around (cx[k], cy[k]), distances measured on the
+ * periodic grid.  The reference's 5-cell nucleus (src/Kobayashi.cpp:116-123) is
+ * the disk of radius 1.  Counters back to 0. */
+KG_API int kg_seed_disks(kg_sim* h, int n, const int* cx, const int* cy, const int* r);
+
+/* Parameter mutation (the reference mutates its float& slider targets,
+ * src/Kobayashi.cpp:579-611). */
+KG_API int kg_set_params(kg_sim* h, const kg_params* p);
+KG_API int kg_get_params(const kg_sim* h, kg_params* p);
+
+/* nsteps explicit Euler steps (_computeGradientLaplacian + _evolution,
+ * src/Kobayashi.cpp:125-221), enqueued on the handle's stream, in CUDA-graph
+ * chunks (kg_set_graph_chunk). */
+KG_API int kg_step(kg_sim* h, long long nsteps);
+
+/* iUpdate (src/Kobayashi.cpp:227-239): 10 steps and frame += 1. */
+KG_API int kg_update(kg_sim* h);
+
+/* Waits for the handle's stream; reports any asynchronous CUDA error. */
+KG_API int kg_sync(kg_sim* h);
+
+/* Host copies of the current state (synchronous); any pointer may be NULL. */
+KG_API int kg_get_fields(kg_sim* h, double* phi, double* T, double* theta);
+/* Overwrite the current state from host buffers (synchronous); NULL leaves a field as is. */
+KG_API int kg_set_fields(kg_sim* h, const double* phi, const double* T, const double* theta);
+
+/* iGetObjectCount (src/Kobayashi.cpp:363-366) */
+KG_API int kg_get_size(const kg_sim* h, int* nx, int* ny);
+/* steps taken since create/reset; frames = iUpdate calls (_simFrame, src/Kobayashi.h:81) */
+KG_API int kg_get_counters(const kg_sim* h, long long* steps, long long* frames);
+
+/* Device pointers of the current state (valid until the next step or reset)
+ * and the handle's cudaStream_t, for consumers that stay on the GPU. */
+KG_API int kg_device_fields(kg_sim* h, double** phi, double** T, double** theta);
+KG_API int kg_get_stream(kg_sim* h, void** stream);
+
+/* Steps per captured CUDA graph used by kg_step (default 100; 0 = no graphs). */
+KG_API int kg_set_graph_chunk(kg_sim* h, int chunk);
+
+/* Message of the calling thread's last failure ("" if none). */
+KG_API const char* kg_last_error(void);
+
+/* Build/version string of the library. */
+KG_API const char* kg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KOBAYASHI_GPU_H */

@@ -1,0 +1,183 @@
+/*
+ * ko_oracle.c -- TEST INFRASTRUCTURE ONLY (the "O2" oracle).
+ *
+ * A plain-C, FP64 restatement of the reference's Kobayashi time step
+ * (jklae/CrystalGrowth src/Kobayashi.cpp), used by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker.
+ * It is never linked into the product library.
+ *
+ * It follows the reference loop by loop and operation by operation, so that,
+ * with the C library's atan/sin/cos selected (libm = 1), it reproduces the
+ * FP64 build of the reference's own code bit for bit:
+ *   stage 1  _computeGradientLaplacian   src/Kobayashi.cpp:125-175
+ *   stage 2  _evolution (in place)       src/Kobayashi.cpp:177-221
+ * The only extension is theta0, the preferred growth angle: the anisotropy
+ * argument is aniso*(theta - theta0), which is bit-identical to the
+ * reference's aniso*theta when theta0 == 0.
+ *
+ * With libm = 0 the elementary functions come from kg_math.h, the definitions
+ * the GPU kernels share; that is the configuration the GPU is compared with.
+ * Build with -ffp-contract=off (no fused multiply-add contraction).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include "../crystalgrowth_gb300/csrc/kg_math.h"
+
+typedef struct ko_params {
+    double dx, dy, dt;
+    double tau, eps_bar, mu, K, delta, aniso, alpha, gamma, teq;
+    double theta0;
+} ko_params;
+
+/* FLT_EPSILON (src/Kobayashi.cpp:154-167) as a double: 2^-23 */
+#define KO_FLT_EPS 0x1p-23
+
+static inline double ko_atan(double x, int libm) { return libm ? atan(x) : kg_atan(x); }
+
+static inline void ko_sincos(double x, double* s, double* c, int libm)
+{
+    if (libm) {
+        *s = sin(x);
+        *c = cos(x);
+    } else {
+        kg_sincos(x, s, c);
+    }
+}
+
+/* periodic neighbour indices, src/Kobayashi.cpp:133-136 */
+#define KO_WRAP(i, n) (((i) % (n) + (n)) % (n))
+
+static void ko_stage1(int nx, int ny, const ko_params* p, const double* phi, const double* t, double* angl,
+                      double* gpx, double* gpy, double* lphi, double* lt, double* eps, double* epsd, int libm,
+                      int nthreads)
+{
+    const double pi = KG_PI; /* PI_F: DXViewer's constant is not vendored; RN(pi) */
+    (void)nthreads;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int j = 0; j < ny; j++) {
+        for (int i = 0; i < nx; i++) {
+            int ip = (i + 1) % nx;
+            int im = ((i - 1) + nx) % nx;
+            int jp = (j + 1) % ny;
+            int jm = ((j - 1) + ny) % ny;
+            size_t c = (size_t)i + (size_t)nx * j;
+#define P(a, b) phi[(size_t)(a) + (size_t)nx * (b)]
+#define TT(a, b) t[(size_t)(a) + (size_t)nx * (b)]
+            gpx[c] = (P(ip, j) - P(im, j)) / p->dx;
+            gpy[c] = (P(i, jp) - P(i, jm)) / p->dy;
+            lphi[c] = (2.0 * (P(ip, j) + P(im, j) + P(i, jp) + P(i, jm)) + P(ip, jp) + P(im, jm) + P(im, jp) +
+                       P(ip, jm) - 12.0 * P(i, j)) /
+                      (3.0 * p->dx * p->dx);
+            lt[c] = (2.0 * (TT(ip, j) + TT(im, j) + TT(i, jp) + TT(i, jm)) + TT(ip, jp) + TT(im, jm) + TT(im, jp) +
+                     TT(ip, jm) - 12.0 * TT(i, j)) /
+                    (3.0 * p->dx * p->dx);
+#undef P
+#undef TT
+            double gx = gpx[c], gy = gpy[c];
+            if (gx <= +KO_FLT_EPS && gx >= -KO_FLT_EPS) {
+                if (gy < -KO_FLT_EPS)
+                    angl[c] = -0.5 * pi;
+                else if (gy > +KO_FLT_EPS)
+                    angl[c] = 0.5 * pi;
+            }
+            if (gx > +KO_FLT_EPS) {
+                if (gy < -KO_FLT_EPS)
+                    angl[c] = 2.0 * pi + ko_atan(gy / gx, libm);
+                else if (gy > +KO_FLT_EPS)
+                    angl[c] = ko_atan(gy / gx, libm);
+            }
+            if (gx < -KO_FLT_EPS)
+                angl[c] = pi + ko_atan(gy / gx, libm);
+
+            double s, co;
+            ko_sincos(p->aniso * (angl[c] - p->theta0), &s, &co, libm);
+            eps[c] = p->eps_bar * (1.0 + p->delta * co);
+            epsd[c] = -p->eps_bar * p->aniso * p->delta * s;
+        }
+    }
+}
+
+static void ko_stage2(int nx, int ny, const ko_params* p, double* phi, double* t, const double* gpx,
+                      const double* gpy, const double* lphi, const double* lt, const double* eps,
+                      const double* epsd, int libm, int nthreads)
+{
+    const double pi = KG_PI;
+    (void)nthreads;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int j = 0; j < ny; j++) {
+        for (int i = 0; i < nx; i++) {
+            size_t ip = (size_t)((i + 1) % nx) + (size_t)nx * j;
+            size_t im = (size_t)(((i - 1) + nx) % nx) + (size_t)nx * j;
+            size_t jp = (size_t)i + (size_t)nx * ((j + 1) % ny);
+            size_t jm = (size_t)i + (size_t)nx * (((j - 1) + ny) % ny);
+            size_t c = (size_t)i + (size_t)nx * j;
+
+            double gradEpsPowX = (eps[ip] * eps[ip] - eps[im] * eps[im]) / p->dx;
+            double gradEpsPowY = (eps[jp] * eps[jp] - eps[jm] * eps[jm]) / p->dy;
+            double term1 = (eps[jp] * epsd[jp] * gpx[jp] - eps[jm] * epsd[jm] * gpx[jm]) / p->dy;
+            double term2 = -(eps[ip] * epsd[ip] * gpy[ip] - eps[im] * epsd[im] * gpy[im]) / p->dx;
+            double term3 = gradEpsPowX * gpx[c] + gradEpsPowY * gpy[c];
+            double m = p->alpha / pi * ko_atan(p->gamma * (p->teq - t[c]), libm);
+            double oldPhi = phi[c];
+            double oldT = t[c];
+            phi[c] = phi[c] + (term1 + term2 + eps[c] * eps[c] * lphi[c] + term3 +
+                               oldPhi * (1.0 - oldPhi) * (oldPhi - 0.5 + m)) *
+                                  p->dt / p->tau;
+            t[c] = oldT + lt[c] * p->dt + p->K * (phi[c] - oldPhi);
+        }
+    }
+}
+
+/*
+ * Advance (phi, T, theta) in place by nsteps explicit steps.
+ * libm = 1: C library atan/sin/cos (the reference's own math);
+ * libm = 0: kg_math.h (the GPU's math).  Returns 0, or -1 on bad input.
+ */
+int ko_run(int nx, int ny, const ko_params* p, double* phi, double* t, double* theta, long long nsteps, int libm,
+           int nthreads)
+{
+    if (nx < 1 || ny < 1 || !p || !phi || !t || !theta || nsteps < 0)
+        return -1;
+    if (nthreads < 1)
+        nthreads = 1;
+    size_t n = (size_t)nx * (size_t)ny;
+    double* w = (double*)malloc(6 * n * sizeof(double));
+    if (!w)
+        return -1;
+    memset(w, 0, 6 * n * sizeof(double));
+    double *gpx = w, *gpy = w + n, *lphi = w + 2 * n, *lt = w + 3 * n, *eps = w + 4 * n, *epsd = w + 5 * n;
+    for (long long s = 0; s < nsteps; s++) {
+        ko_stage1(nx, ny, p, phi, t, theta, gpx, gpy, lphi, lt, eps, epsd, libm, nthreads);
+        ko_stage2(nx, ny, p, phi, t, gpx, gpy, lphi, lt, eps, epsd, libm, nthreads);
+    }
+    free(w);
+    return 0;
+}
+
+/* kg_math.h entry points, for the elementary-function tests */
+double ko_kg_atan(double x) { return kg_atan(x); }
+void ko_kg_sincos(double x, double* s, double* c) { kg_sincos(x, s, c); }
+double ko_kg_cdiv(double a, double b)
+{
+    double yh, yl;
+    if (kg_cdiv_prepare(b, &yh, &yl))
+        return a / b;
+    return kg_cdiv(a, b, yh, yl);
+}
+/* n quotients a[i] / b through kg_cdiv; returns how many differ in bits from a[i] / b */
+long long ko_kg_cdiv_check(const double* a, long long n, double b)
+{
+    double yh, yl;
+    if (kg_cdiv_prepare(b, &yh, &yl))
+        return -1;
+    long long bad = 0;
+    for (long long i = 0; i < n; i++) {
+        double q = kg_cdiv(a[i], b, yh, yl);
+        double r = a[i] / b;
+        if (kg_bits(q) != kg_bits(r))
+            bad++;
+    }
+    return bad;
+}

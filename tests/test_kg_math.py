@@ -1,0 +1,116 @@
+"""kg_math.h (host build): faithful atan / sin / cos, and kg_cdiv == IEEE division.
+
+These functions are shared source between the CUDA kernels and the CPU
+oracle; the GPU tests check the device build against the same values.
+"""
+import math
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+import ko_oracle
+
+mp = pytest.importorskip("mpmath")
+mp.mp.prec = 200
+
+
+def ulp_err(got, exact):
+    e = float(exact)
+    if e == 0.0:
+        return 0.0 if got == 0.0 else math.inf
+    return float(abs(mp.mpf(got) - exact) / math.ulp(e))
+
+
+def test_atan_faithful_random():
+    rng = np.random.default_rng(11)
+    xs = np.concatenate([rng.uniform(-1, 1, 3000), rng.uniform(-20, 20, 3000),
+                         10.0 ** rng.uniform(-12, 12, 3000) * rng.choice([-1, 1], 3000),
+                         rng.uniform(9.5, 10.5, 1000), 1.0 + rng.uniform(-1e-9, 1e-9, 500)])
+    worst = max(ulp_err(ko_oracle.kg_atan(x), mp.atan(mp.mpf(float(x)))) for x in xs)
+    assert worst < 1.0
+
+
+def test_atan_special_values():
+    a = ko_oracle.kg_atan
+    assert a(0.0) == 0.0 and math.copysign(1, a(0.0)) == 1
+    assert a(-0.0) == 0.0 and math.copysign(1, a(-0.0)) == -1
+    assert a(math.inf) == math.pi / 2 and a(-math.inf) == -math.pi / 2
+    assert math.isnan(a(math.nan))
+    assert a(1e300) == math.pi / 2
+    assert a(1.0) == math.atan(1.0)
+    assert a(-1.0) == -math.atan(1.0)
+    assert a(5e-324) == 5e-324
+    for x in (0.5, 2.0, 10.0, 1e-8, 123.0):
+        assert a(-x) == -a(x)
+
+
+def test_sincos_faithful_random():
+    rng = np.random.default_rng(12)
+    xs = np.concatenate([rng.uniform(-60, 60, 5000), rng.uniform(-4000, 4000, 1000), rng.uniform(-1e-3, 1e-3, 500),
+                         np.arange(-64, 65) * (math.pi / 128)])
+    ws = wc = 0.0
+    for x in xs:
+        s, c = ko_oracle.kg_sincos(x)
+        ws = max(ws, ulp_err(s, mp.sin(mp.mpf(float(x)))))
+        wc = max(wc, ulp_err(c, mp.cos(mp.mpf(float(x)))))
+    assert ws < 1.0 and wc < 1.0
+
+
+def test_sincos_domain():
+    s, c = ko_oracle.kg_sincos(0.0)
+    assert s == 0.0 and c == 1.0
+    for x in (4096.0, -4096.0, 1e10, math.inf, math.nan):
+        s, c = ko_oracle.kg_sincos(x)
+        assert math.isnan(s) and math.isnan(c)
+
+
+@pytest.mark.parametrize("b", [0.03, 3 * 0.03 * 0.03, 3e-4, 2e-4, 4e-4, 1e-4, 0.1, 7.0, 1 / 3, 0.0270000001, 2.0 ** -99])
+def test_cdiv_matches_ieee_random(b):
+    rng = np.random.default_rng(int(b * 1e6) % 1000 + 1)
+    n = 1_000_000
+    a = np.concatenate([rng.standard_normal(n) * 10.0 ** rng.integers(-300, 300, n),
+                        rng.uniform(-1, 1, n),
+                        rng.integers(1, 2 ** 53, n).astype(np.float64) * 2.0 ** -60,
+                        np.array([0.0, -0.0, 5e-324, -5e-324, 2.0 ** -900, 2.0 ** -899, 2.0 ** 900, 1e308, math.inf,
+                                  -math.inf, math.nan])])
+    assert ko_oracle.kg_cdiv_mismatches(a, b) == 0
+
+
+def _rn(x, p):
+    """round a rational to the nearest p-bit binary float, ties to even (unbounded exponent)"""
+    if x == 0:
+        return Fraction(0)
+    s = -1 if x < 0 else 1
+    x = abs(x)
+    e = x.numerator.bit_length() - x.denominator.bit_length()
+    if Fraction(2) ** e > x:
+        e -= 1
+    scale = Fraction(2) ** (e - p + 1)
+    m = x / scale
+    fl = m.numerator // m.denominator
+    rem = m - fl
+    if rem > Fraction(1, 2) or (rem == Fraction(1, 2) and fl % 2 == 1):
+        fl += 1
+    return s * fl * scale
+
+
+@pytest.mark.parametrize("p", [6, 7, 8, 9, 10])
+def test_cdiv_algorithm_exhaustive_small_precision(p):
+    """The kg_cdiv sequence (hi+lo reciprocal, faithful quotient, Markstein
+    correction) run in p-bit arithmetic returns RN(a/b) for every pair of
+    p-bit significands: the same argument as for p = 53, checked exhaustively."""
+    lo, hi = 2 ** (p - 1), 2 ** p
+    for B in range(lo, hi):
+        b = Fraction(B, lo)
+        yh = _rn(1 / b, p)
+        e = _rn(1 - b * yh, p)
+        assert e == 1 - b * yh  # exact, as the C code relies on
+        yl = _rn(e / b, p)
+        for A in range(lo, hi):
+            a = Fraction(A, lo)
+            q0 = _rn(a * yh + _rn(a * yl, p), p)
+            r = _rn(a - q0 * b, p)
+            assert r == a - q0 * b  # the remainder is exact
+            q = _rn(q0 + r * yh, p)
+            assert q == _rn(a / b, p), (A, B)
