@@ -1,0 +1,303 @@
+"""Benchmark of the fused Kobayashi step on GB300 (FP64 cell-updates/s).
+
+Workload (the spec throughput case): one 8192 x 8192 FP64 grid, 64
+seeded disks of radius 4..8, reference parameters with delta = 0.02 and
+theta0 = 0.2; the state advances in CUDA-graph chunks of 100 explicit steps.
+One bench step = one chunk = 100 time steps = 6.71e9 cell-updates.  The
+state is 3.2 GB (two copies of phi, T, theta), far above the 129 MB L2, so no
+flush is needed between timed chunks.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's own CPU step (src/Kobayashi.cpp built
+unmodified in FP64 by oracle/build_oracle.py; the restated oracle if that
+build is absent) on the host, one time step of the same 8192^2 state per
+bench step.  Under torchrun with N > 1 every rank runs an independent replica
+(the grid is not sharded: one GPU per box), rank 0 prints.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CHUNK = 100
+BYTES_PER_CELL = 48  # phi, T, theta: FP64, read once and written once
+
+
+def dist_init(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("KG_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples of the SM clock and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.proc = None
+        self.device = device
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        rows = []
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 7:
+                try:
+                    rows.append((float(f[0]), float(f[1]), f[3:7]))
+                except ValueError:
+                    pass
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for _, _, fl in rows for k, v in enumerate(fl) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the step kernel from the committed ncu summary (null if absent)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "kg_step_kernel_traffic.json")) as f:
+            d = json.load(f)
+        return d.get("bytes_per_launch_8192"), d
+    except (OSError, ValueError):
+        return None, None
+
+
+def cpu_baseline_sample(cfg, seconds_budget=20.0):
+    """The reference's own FP64 step on the host: 8192^2 state from the workload, whole time steps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import ko_oracle
+    from crystalgrowth_gb300 import configs
+    nx, ny = cfg["nx"], cfg["ny"]
+    init = configs.initial_fields(nx, ny, cfg["disks"])
+    p = dict(cfg["params"])
+    try:
+        r = ko_oracle.Reference(nx, ny, p["dt"], fp64=True)
+        kind = "reference"
+        p_ref = dict(p)  # the reference has no theta0; its step is timed with the same field sizes
+        r.set_params(p_ref)
+        r.set_state(*init)
+        step = r.step
+    except (FileNotFoundError, OSError):
+        kind = "port"
+        state = list(init)
+
+        def step(n):
+            state[:] = ko_oracle.port_run(*state, p, n, libm=True, threads=1)
+    t0 = time.perf_counter()
+    step(1)
+    t1 = time.perf_counter()
+    n_steps = 1
+    per = t1 - t0
+    extra = max(0, int(seconds_budget / max(per, 1e-3)) - 1)
+    extra = min(extra, 4)
+    if extra:
+        t2 = time.perf_counter()
+        step(extra)
+        per = (time.perf_counter() - t2) / extra
+        n_steps += extra
+    return {"value": nx * ny / per, "unit": "cell-updates/s", "cores": 1, "kind": kind,
+            "sample": "%d time step(s) of the %dx%d FP64 state, single thread (the reference is single-threaded)"
+                      % (n_steps, nx, ny)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ko_oracle
+    from crystalgrowth_gb300 import configs
+    cfg = configs.grid_8192()
+    nx, ny = cfg["nx"], cfg["ny"]
+    init = configs.initial_fields(nx, ny, cfg["disks"])
+    try:
+        r = ko_oracle.Reference(nx, ny, cfg["params"]["dt"], fp64=True)
+        r.set_params(cfg["params"])
+        r.set_state(*init)
+        step = r.step
+        kind = "reference"
+    except (FileNotFoundError, OSError):
+        kind = "port"
+        state = list(init)
+
+        def step(n):
+            state[:] = ko_oracle.port_run(*state, cfg["params"], n, libm=True, threads=1)
+    for _ in range(args.warmup):
+        step(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step(1)
+    dt = time.perf_counter() - t0
+    value = nx * ny * args.steps / dt
+    line = {"impl": "reference", "metric": "fp64_cell_updates_per_s", "value": value, "unit": "cell-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "grid_8192: 8192x8192 FP64 Kobayashi step, 64 seeded disks r=4..8",
+                       "bench_step": "1 time step on the host (reference CPU path)", "disks_seed": 8192},
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": 1, "kind": kind,
+                             "sample": "%d timed time steps of the 8192^2 state, single thread" % args.steps},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world):
+    import numpy as np
+    import torch
+    from crystalgrowth_gb300 import Kobayashi, configs
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    cfg = configs.grid_8192(n=args.grid, n_disks=args.disks)
+    nx, ny = cfg["nx"], cfg["ny"]
+    cells = nx * ny
+    sim = Kobayashi(nx, ny, cfg["params"]["dt"], params=cfg["params"])
+    sim.seed_disks(cfg["disks"])
+    sim.set_graph_chunk(CHUNK)
+    stream = torch.cuda.ExternalStream(sim.stream())
+
+    # warm-up chunks (the trajectory continues from here)
+    for _ in range(args.warmup):
+        sim.step(CHUNK)
+    sim.sync()
+
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        sim.step(CHUNK)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(ms, world)
+    ms_per_step = ms / args.steps
+    value = world * cells * CHUNK * args.steps / (ms / 1e3)
+    launch_s = ms_per_step / 1e3 / CHUNK  # average duration of one step-kernel launch
+
+    # end to end through the C ABI with host buffers: upload state, 100 steps, download state
+    pinned = [torch.empty((ny, nx), dtype=torch.float64, pin_memory=True) for _ in range(3)]
+    host = [t.numpy() for t in pinned]
+    for h, v in zip(host, sim.fields()):
+        h[...] = v
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.set_fields(*host)
+        sim.step(CHUNK)
+        out = sim.fields()
+        for h, v in zip(host, out):
+            h[...] = v
+    t1 = time.perf_counter()
+    e2e_s = max_over_ranks(t1 - t0, world)
+    e2e_value = world * cells * CHUNK * e2e_steps / e2e_s
+
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_CELL * cells / launch_s / 1e9
+    traffic, _ = profile_traffic()
+    line = {"metric": "fp64_cell_updates_per_s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "grid_%d: %dx%d FP64 Kobayashi step, %d seeded disks r=4..8, "
+                                   "delta=0.02 theta0=0.2" % (nx, nx, ny, args.disks),
+                       "bench_step": "one CUDA graph of %d time steps" % CHUNK,
+                       "steps_timed": "time steps %d..%d of the trajectory" % (args.warmup * CHUNK,
+                                                                             (args.warmup + args.steps) * CHUNK),
+                       "l2": "inputs larger than L2 (3.2 GB state)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "note": "48 B/cell algorithmic; the kernel is FP64-pipe bound on GB300"},
+            "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": 3 * 8 * cells,
+                    "d2h_bytes_per_step": 3 * 8 * cells},
+            "gpu_launches": args.steps * CHUNK,
+            "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(cfg)
+    sim.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, default=8192, help="side of the square grid (8192 = the benchmark workload)")
+    ap.add_argument("--disks", type=int, default=64)
+    args = ap.parse_args()
+    rank, world = dist_init(args.gpus)
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -71,6 +71,21 @@ _SIGS = {
     "kg_set_graph_chunk": [_vp, ctypes.c_int],
     "kg_last_error": [],
     "kg_version": [],
+    "kg_diag_eval": [ctypes.c_int, _dp, _dp, ctypes.c_longlong, ctypes.c_double],
+    "kg_diag_barrier_timeout": [ctypes.c_int, ctypes.c_longlong, _ip],
+    "kg_batch_create": [ctypes.c_int, _ip, _ip, ctypes.POINTER(Params), ctypes.POINTER(_vp)],
+    "kg_batch_destroy": [_vp],
+    "kg_batch_seed_disks": [_vp, ctypes.c_int, ctypes.c_int, _ip, _ip, _ip],
+    "kg_batch_step": [_vp, ctypes.c_longlong],
+    "kg_batch_sync": [_vp],
+    "kg_batch_get_fields": [_vp, ctypes.c_int, _dp, _dp, _dp],
+    "kg_batch_set_fields": [_vp, ctypes.c_int, _dp, _dp, _dp],
+    "kg_batch_get_info": [_vp, _ip, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), _ip],
+    "kg_batch_set_tuning": [_vp, _vp],
+    "kg_batch_get_tuning": [_vp, _vp],
+    "kg_batch_autotune": [_vp, ctypes.c_int, _vp, ctypes.POINTER(ctypes.c_double)],
+    "kg_batch_get_stream": [_vp, ctypes.POINTER(_vp)],
+    "kg_diag_fp64_peak": [ctypes.POINTER(ctypes.c_double)],
 }
 _RESTYPE = {"kg_last_error": ctypes.c_char_p, "kg_version": ctypes.c_char_p}
 

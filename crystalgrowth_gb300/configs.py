@@ -57,16 +57,16 @@ def grid_300():
     return dict(name="grid_300", nx=300, ny=300, params=dict(BASE), disks=[(150, 150, 5)], steps=2000)
 
 
-def grid_8192(seed=8192, n_disks=64):
+def grid_8192(seed=8192, n_disks=64, n=8192):
+    """the 8192^2 throughput case; other n give the same recipe on an n^2 grid (profiling cases)"""
     rng = SplitMix64(seed)
-    n = 8192
     disks = []
     while len(disks) < n_disks:
         cx, cy, r = rng.randint(0, n - 1), rng.randint(0, n - 1), rng.randint(4, 8)
         ok = all(math.hypot(periodic_dist2(cx, x, n), periodic_dist2(cy, y, n)) > r + rr for x, y, rr in disks)
         if ok:
             disks.append((cx, cy, r))
-    return dict(name="grid_8192", nx=n, ny=n, params=dict(BASE), disks=disks, steps=10000, chunk=100)
+    return dict(name="grid_%d" % n, nx=n, ny=n, params=dict(BASE), disks=disks, steps=10000, chunk=100)
 
 
 def variants_2048(steps=5000):

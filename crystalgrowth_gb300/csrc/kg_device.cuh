@@ -70,18 +70,23 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
     double gx = kg_cdiv(pE - pW, P.dx, P.rdx_h, P.rdx_l);
     double gy = kg_cdiv(pN - pS, P.dy, P.rdy_h, P.rdy_l);
     uint64_t bx = kg_bits(gx), by = kg_bits(gy);
-    if (kg_small(bx)) {
-        if (kg_neg_big(by))
+    /* the reference's three branches (src/Kobayashi.cpp:154-167) with one
+     * shared atan call, so that lanes on different branches do not run it
+     * one after the other; theta = off + atan(gy/gx), off in {0, pi, 2 pi}
+     * (for off = 0 the atan value itself: adding +0 could turn -0 into +0) */
+    bool gx_small = kg_small(bx), gx_pos = kg_pos_big(bx), gx_neg = kg_neg_big(bx);
+    bool gy_pos = kg_pos_big(by), gy_neg = kg_neg_big(by);
+    if (gx_small) {
+        if (gy_neg)
             theta = -0.5 * KG_PI;
-        else if (kg_pos_big(by))
+        else if (gy_pos)
             theta = 0.5 * KG_PI;
-    } else if (kg_pos_big(bx)) {
-        if (kg_neg_big(by))
-            theta = 2.0 * KG_PI + kg_atan(gy / gx);
-        else if (kg_pos_big(by))
-            theta = kg_atan(gy / gx);
-    } else if (kg_neg_big(bx)) {
-        theta = KG_PI + kg_atan(gy / gx);
+    }
+    bool use_atan = gx_neg || (gx_pos && (gy_pos || gy_neg));
+    if (use_atan) {
+        double at = kg_atan(gy / gx);
+        double s = (gx_neg ? KG_PI : 2.0 * KG_PI) + at;
+        theta = (gx_neg || gy_neg) ? s : at;
     }
     double arg = P.aniso * (theta - P.theta0);
     double e2, ee;

@@ -24,8 +24,8 @@
  *             correction q = q0 + (a - b q0) * RN(1/b) applied to a faithful
  *             quotient q0 = a * (1/b as a hi+lo pair); returns RN(a/b), i.e.
  *             the same bits as the IEEE division a/b (Markstein 1990; the
- *             hi+lo reciprocal makes q0 faithful).  Operands outside
- *             [2^-900, 2^900] in magnitude fall back to a/b.
+ *             hi+lo reciprocal makes q0 faithful).  Subnormal, huge and
+ *             non-finite dividends fall back to a/b.
  *
  * Accuracy: kg_atan and kg_sincos are faithful (error < 1 ulp) on the
  * documented domains; kg_sincos requires |x| < 4096 and returns NaN outside.
@@ -247,17 +247,29 @@ KG_HD int kg_cdiv_prepare(double b, double* yh, double* yl)
 
 /*
  * a / b with the bits of the IEEE division, for a divisor b prepared by
- * kg_cdiv_prepare.  4 double operations instead of the ~8 of a general
- * division.  Zero, tiny (< 2^-900), huge (>= 2^900), infinite and NaN
- * dividends take the IEEE division itself.
+ * kg_cdiv_prepare: 4 double operations instead of the ~8 of a general
+ * division.  Normal dividends below 2^899 take this path -- those under
+ * 2^-900 lifted by 2^200 first and the quotient scaled back (both exact
+ * exponent-field adjustments) -- and so do zeros (0/b = 0 with a's sign);
+ * subnormal, huge, infinite and NaN dividends, and tiny dividends whose
+ * quotient would be subnormal, take the IEEE division itself.
  */
 KG_HD double kg_cdiv(double a, double b, double yh, double yl)
 {
-    uint64_t ea = (kg_bits(a) >> 52) & 0x7ff;
-    if (ea - (1023u - 900u) < 1800u) {
-        double q0 = kg_fma(a, yh, a * yl);
-        double r = kg_fma(-q0, b, a);
-        return kg_fma(r, yh, q0);
+    uint64_t ua = kg_bits(a);
+    uint64_t ea = (ua >> 52) & 0x7ff;
+    int zero = (ua & 0x7fffffffffffffffull) == 0;
+    if (ea - 1u < 1921u || zero) {
+        uint64_t sh = (ea < 123u) ? (200ull << 52) : 0ull;
+        double as = kg_from_bits(ua + sh);
+        double q0 = kg_fma(as, yh, as * yl);
+        double r = kg_fma(-q0, b, as);
+        double q = kg_fma(r, yh, q0);
+        uint64_t uq = kg_bits(q);
+        if (zero)
+            return a;
+        if (sh == 0 || ((uq >> 52) & 0x7ff) > 200u)
+            return kg_from_bits(uq - sh);
     }
     return a / b;
 }

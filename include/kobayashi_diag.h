@@ -1,0 +1,36 @@
+/*
+ * kobayashi_diag.h -- diagnostic entry points of libkobayashi_gpu.so.
+ *
+ * Not part of the reference's surface (jklae/CrystalGrowth has no
+ * counterpart): they let tests check the device build of kg_math.h against
+ * the host build, and let the benchmark measure the FP64 pipe it is bound by.
+ */
+#ifndef KOBAYASHI_DIAG_H
+#define KOBAYASHI_DIAG_H
+#include "kobayashi_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KG_FN_ATAN 0  /* y = kg_atan(x) */
+#define KG_FN_SIN 1   /* y = sin part of kg_sincos(x) */
+#define KG_FN_COS 2   /* y = cos part of kg_sincos(x) */
+#define KG_FN_CDIV 3  /* y = kg_cdiv(x, b): x / b through the constant-divisor path */
+#define KG_FN_DIV 4   /* y = x / b, the GPU's own IEEE division */
+
+/* Evaluates function `fn` on n host values on the current device (synchronous). */
+KG_API int kg_diag_eval(int fn, const double* x, double* y, long long n, double b);
+
+/* Runs the batched kernel's bounded grid barrier on `blocks` CTAs while it
+ * waits for one CTA more: every wait must give up after max_polls polls.
+ * *timed_out = 1 when the error flag was raised (the expected outcome). */
+KG_API int kg_diag_barrier_timeout(int blocks, long long max_polls, int* timed_out);
+
+/* Measures the FP64 FMA throughput of the current device: lane-operations per second. */
+KG_API int kg_diag_fp64_peak(double* ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

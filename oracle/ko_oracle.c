@@ -181,3 +181,23 @@ long long ko_kg_cdiv_check(const double* a, long long n, double b)
     }
     return bad;
 }
+
+/* host evaluation of kg_math.h over an array: fn 0 atan, 1 sin, 2 cos, 3 kg_cdiv(x, b), 4 x / b */
+int ko_kg_eval(int fn, const double* x, double* y, long long n, double b)
+{
+    double yh = 0, yl = 0;
+    if ((fn == 3 || fn == 4) && kg_cdiv_prepare(b, &yh, &yl))
+        return -1;
+    for (long long i = 0; i < n; i++) {
+        double s, c;
+        switch (fn) {
+        case 0: y[i] = kg_atan(x[i]); break;
+        case 1: kg_sincos(x[i], &s, &c); y[i] = s; break;
+        case 2: kg_sincos(x[i], &s, &c); y[i] = c; break;
+        case 3: y[i] = kg_cdiv(x[i], b, yh, yl); break;
+        case 4: y[i] = x[i] / b; break;
+        default: return -1;
+        }
+    }
+    return 0;
+}

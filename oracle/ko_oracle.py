@@ -56,6 +56,8 @@ def port_lib():
         lib.ko_kg_cdiv.restype = ctypes.c_double
         lib.ko_kg_cdiv_check.argtypes = [_dp, ctypes.c_longlong, ctypes.c_double]
         lib.ko_kg_cdiv_check.restype = ctypes.c_longlong
+        lib.ko_kg_eval.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_longlong, ctypes.c_double]
+        lib.ko_kg_eval.restype = ctypes.c_int
         _port_lib = lib
     return _port_lib
 
@@ -87,6 +89,15 @@ def kg_sincos(x):
     c = ctypes.c_double()
     port_lib().ko_kg_sincos(float(x), ctypes.byref(s), ctypes.byref(c))
     return s.value, c.value
+
+
+def kg_eval(fn, x, b=1.0):
+    """host kg_math over an array: fn 0 atan, 1 sin, 2 cos, 3 kg_cdiv(x, b), 4 x / b"""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    if port_lib().ko_kg_eval(int(fn), _ptr(x), _ptr(y), x.size, float(b)) != 0:
+        raise ValueError("ko_kg_eval failed")
+    return y
 
 
 def kg_cdiv_mismatches(a, b):

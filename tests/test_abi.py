@@ -1,0 +1,85 @@
+"""The C ABI library (CPU-only checks: no CUDA call is made here).
+
+libkobayashi_gpu.so must load and export every function that
+include/*.h declares; the host-only entry points (defaults, validation,
+error text, version) must behave.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+import crystalgrowth_gb300 as kg
+from crystalgrowth_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", h)).read()
+            names |= set(re.findall(r"^KG_API\s+[\w\s\*]*?\b(kg_\w+)\s*\(", text, flags=re.M))
+    return sorted(names)
+
+
+def test_header_declares_the_abi():
+    names = declared_symbols()
+    for must in ("kg_create", "kg_destroy", "kg_step", "kg_update", "kg_reset", "kg_get_fields", "kg_set_fields",
+                 "kg_set_params", "kg_last_error"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = kg.load()
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (kg_\w+)", out))
+    assert set(declared_symbols()) <= exported
+
+
+def test_python_binding_covers_every_symbol():
+    assert set(declared_symbols()) <= set(_lib._SIGS) | {"kg_version"}
+
+
+def test_defaults_are_the_reference_defaults():
+    p = kg.Params.make()
+    d = p.as_dict()
+    # src/Kobayashi.cpp:61-63 and 76-84
+    assert d == dict(dx=0.03, dy=0.03, dt=1e-4, tau=0.0003, eps_bar=0.010, mu=1.0, K=1.6, delta=0.05, aniso=6.0,
+                     alpha=0.9, gamma=10.0, teq=1.0, theta0=0.0)
+
+
+@pytest.mark.parametrize("field,value", [("dx", 0.0), ("dy", -1.0), ("tau", 0.0), ("dt", 0.0), ("eps_bar", 0.0),
+                                         ("aniso", 2.5), ("aniso", 0.0), ("theta0", 1e3), ("delta", float("nan")),
+                                         ("K", float("inf"))])
+def test_validation_rejects(field, value):
+    lib = kg.load()
+    p = kg.Params.make(**{field: value})
+    assert lib.kg_params_validate(ctypes.byref(p)) == _lib.KG_ERR_INVALID
+    assert len(lib.kg_last_error()) > 0
+
+
+def test_validation_accepts_slider_ranges():
+    """every value the reference's sliders can reach (src/Kobayashi.cpp:12-59) is a valid parameter"""
+    lib = kg.load()
+    for tau in (1e-4, 9e-4):
+        for eb in (0.006, 0.015):
+            for K in (1.0, 1.9):
+                for delta in (0.01, 0.09):
+                    for j in (2.0, 8.0):
+                        p = kg.Params.make(tau=tau, eps_bar=eb, K=K, delta=delta, aniso=j, alpha=1.2, gamma=20.0,
+                                           teq=1.5)
+                        assert lib.kg_params_validate(ctypes.byref(p)) == 0
+
+
+def test_null_handle_is_an_error_not_a_crash():
+    lib = kg.load()
+    assert lib.kg_step(None, 1) == _lib.KG_ERR_INVALID
+    assert lib.kg_destroy(None) == 0
+    assert b"null" in lib.kg_last_error()
+    assert lib.kg_version().startswith(b"kobayashi-gb300")

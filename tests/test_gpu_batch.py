@@ -1,0 +1,128 @@
+"""Batched ensemble (kg_batch_*): every instance bit-identical to the CPU
+oracle run of the same grid and parameters, in both execution modes and for
+every strip shape the autotuner may choose; the autotuner leaves the state as
+it found it; the bounded grid barrier gives up instead of hanging."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import ko_oracle
+from crystalgrowth_gb300 import Batch, Kobayashi, configs, _lib
+from crystalgrowth_gb300.batch import KG_BATCH_LAUNCH, KG_BATCH_PERSISTENT
+
+pytestmark = pytest.mark.gpu
+
+
+def bits_equal(a, b):
+    return np.array_equal(np.asarray(a, np.float64).view(np.uint64), np.asarray(b, np.float64).view(np.uint64))
+
+
+def small_ensemble(count=24, seed=7, lo=5, hi=300):
+    rng = configs.SplitMix64(seed)
+    inst = []
+    for _ in range(count):
+        nx = rng.randint(lo, hi)
+        ny = rng.randint(lo, hi)
+        p = dict(configs.BASE, delta=rng.uniform(0.01, 0.06), aniso=float(4 if rng.next() & 1 else 6),
+                 K=rng.uniform(1.2, 2.0), theta0=rng.uniform(0.0, 1.5), tau=rng.uniform(2e-4, 4e-4))
+        r = rng.randint(1, max(1, min(nx, ny) // 4))
+        inst.append(dict(nx=nx, ny=ny, params=p, disks=[(nx // 2, ny // 2, r)]))
+    return inst
+
+
+def make_batch(inst):
+    b = Batch([(i["nx"], i["ny"]) for i in inst], [i["params"] for i in inst])
+    for k, i in enumerate(inst):
+        b.seed_disks(k, i["disks"])
+    return b
+
+
+def oracle(inst, steps):
+    return [ko_oracle.port_run(*configs.initial_fields(i["nx"], i["ny"], i["disks"]), i["params"], steps,
+                               threads=8) for i in inst]
+
+
+@pytest.mark.parametrize("mode", [KG_BATCH_LAUNCH, KG_BATCH_PERSISTENT])
+@pytest.mark.parametrize("nt,bh,chunk", [(64, 16, 7), (128, 64, 100), (256, 32, 3)])
+def test_batch_bitwise_vs_oracle(mode, nt, bh, chunk):
+    inst = small_ensemble()
+    steps = 41
+    b = make_batch(inst)
+    b.set_tuning(nt=nt, bh=bh, mode=mode, chunk=chunk)
+    b.step(steps)
+    ref = oracle(inst, steps)
+    for k in range(len(inst)):
+        for x, y in zip(b.fields(k), ref[k]):
+            assert bits_equal(x, y), (k, inst[k]["nx"], inst[k]["ny"])
+    assert b.info()["steps"] == steps
+    b.close()
+
+
+def test_batch_equals_single_grid_runs():
+    inst = small_ensemble(count=6, seed=11, lo=30, hi=200)
+    b = make_batch(inst)
+    b.step(60)
+    for k, i in enumerate(inst):
+        s = Kobayashi(i["nx"], i["ny"], i["params"]["dt"], params=i["params"])
+        s.seed_disks(i["disks"])
+        s.step(60)
+        for x, y in zip(b.fields(k), s.fields()):
+            assert bits_equal(x, y)
+        s.close()
+    b.close()
+
+
+def test_autotune_restores_state_and_keeps_results():
+    inst = small_ensemble(count=10, seed=3)
+    b = make_batch(inst)
+    b.step(5)
+    before = [b.fields(k) for k in range(len(inst))]
+    best, ms = b.autotune(trial_steps=3)
+    assert best["nt"] in (64, 128, 256) and ms > 0
+    after = [b.fields(k) for k in range(len(inst))]
+    for x, y in zip(before, after):
+        for u, v in zip(x, y):
+            assert bits_equal(u, v)
+    assert b.info()["steps"] == 5
+    b.step(20)
+    ref = oracle(inst, 25)
+    for k in range(len(inst)):
+        for x, y in zip(b.fields(k), ref[k]):
+            assert bits_equal(x, y)
+    b.close()
+
+
+def test_ensemble_512_config_truncated():
+    """the 512-instance mixed-size ensemble: a sample of instances checked after 10 steps"""
+    cfg = configs.ensemble_512()
+    inst = cfg["instances"]
+    b = make_batch(inst)
+    b.step(10)
+    for k in (0, 1, 100, 255, 511):
+        ref = ko_oracle.port_run(*configs.initial_fields(inst[k]["nx"], inst[k]["ny"], inst[k]["disks"]),
+                                 inst[k]["params"], 10, threads=8)
+        for x, y in zip(b.fields(k), ref):
+            assert bits_equal(x, y)
+    b.close()
+
+
+def test_barrier_wait_runs_out_and_context_survives():
+    flag = ctypes.c_int(-1)
+    _lib.check(_lib.lib().kg_diag_barrier_timeout(2, 20000, ctypes.byref(flag)))
+    assert flag.value == 1
+    s = Kobayashi(32, 32, 1e-4)  # the context is still usable
+    s.step(3)
+    s.sync()
+    s.close()
+
+
+def test_batch_rejects_bad_input():
+    with pytest.raises(_lib.KgError):
+        Batch([(0, 5)], [dict()])
+    b = Batch([(8, 8)], [dict()])
+    with pytest.raises(_lib.KgError):
+        b.set_tuning(nt=100)
+    with pytest.raises(_lib.KgError):
+        b.fields(3)
+    b.close()

@@ -1,0 +1,58 @@
+"""kg_math.h on the device (sm_103a) against the host build: identical bits.
+
+The kernels and the CPU oracle share these functions as source; this checks
+that nvcc's device build (no FMA contraction, correctly rounded FP32 seed)
+computes the same bits as the host build, on random and edge-case inputs, and
+that the constant-divisor path equals the GPU's own IEEE division.
+"""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+import ko_oracle
+from crystalgrowth_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+
+
+def dev_eval(fn, x, b=1.0):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    _lib.check(_lib.lib().kg_diag_eval(fn, _lib.dptr(x), _lib.dptr(y), x.size, float(b)))
+    return y
+
+
+def inputs(seed, n=2_000_000):
+    rng = np.random.default_rng(seed)
+    edge = np.array([0.0, -0.0, 1.0, -1.0, 5e-324, -5e-324, 2.0 ** -1022, 2.0 ** -900, 2.0 ** -899, 2.0 ** 899,
+                     2.0 ** 64, 2.0 ** 65, 1e300, math.inf, -math.inf, math.nan, 4095.99, -4095.99, 4096.0,
+                     math.pi / 2, math.pi, 1 + 2 ** -52, 1 - 2 ** -53])
+    return np.concatenate([edge, rng.uniform(-2, 2, n), rng.uniform(-70, 70, n),
+                           rng.standard_normal(n) * 10.0 ** rng.integers(-310, 310, n),
+                           rng.uniform(9, 11, n // 4)])
+
+
+def same_bits(a, b):
+    return np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+@pytest.mark.parametrize("fn", [0, 1, 2])
+def test_transcendentals_device_equals_host(fn):
+    x = inputs(100 + fn)
+    assert same_bits(dev_eval(fn, x), ko_oracle.kg_eval(fn, x))
+
+
+@pytest.mark.parametrize("b", [0.03, 3 * 0.03 * 0.03, 3e-4, 2.1e-4, 3.99e-4, 1e-4, 9e-4, 7.0, 1 / 3])
+def test_constant_division_equals_ieee_on_device(b):
+    x = inputs(int(b * 1e7) % 997)
+    dev = dev_eval(3, x, b)
+    assert same_bits(dev, dev_eval(4, x, b))
+    assert same_bits(dev, ko_oracle.kg_eval(4, x, b))
+
+
+def test_fp64_peak_probe():
+    v = ctypes.c_double()
+    _lib.check(_lib.lib().kg_diag_fp64_peak(ctypes.byref(v)))
+    assert v.value > 1e10

@@ -1,0 +1,179 @@
+"""GPU parity of the fused step (libkobayashi_gpu.so through the C ABI) against
+the CPU oracle, which follows src/Kobayashi.cpp:125-221 operation by
+operation.  Integer/byte-exact bar: the FP64 fields must be identical bit for
+bit (tolerance 0); the reference defaults fixture, computed with the C
+library's atan/sin/cos, must agree within the measured noise floor.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import ko_oracle
+from crystalgrowth_gb300 import Kobayashi, KgError, configs
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+THREADS = max(1, min(16, os.cpu_count() or 1))
+
+
+def bits_equal(a, b):
+    return np.array_equal(np.asarray(a, np.float64).view(np.uint64), np.asarray(b, np.float64).view(np.uint64))
+
+
+def gpu_run(nx, ny, params, disks, steps, chunk=None):
+    sim = Kobayashi(nx, ny, params["dt"], params=params)
+    sim.seed_disks(disks)
+    if chunk is not None:
+        sim.set_graph_chunk(chunk)
+    sim.step(steps)
+    out = sim.fields()
+    sim.close()
+    return out
+
+
+def oracle_run(nx, ny, params, disks, steps):
+    return ko_oracle.port_run(*configs.initial_fields(nx, ny, disks), params, steps, libm=False, threads=THREADS)
+
+
+@pytest.mark.parametrize("nx,ny,steps", [(1, 1, 5), (2, 3, 10), (3, 3, 25), (17, 13, 300), (64, 48, 200),
+                                         (126, 64, 60), (127, 65, 60), (130, 70, 200), (253, 129, 100),
+                                         (1000, 777, 40)])
+def test_step_bitwise_small_and_ragged(nx, ny, steps):
+    p = dict(configs.BASE)
+    disks = [(nx // 2, ny // 2, max(1, min(nx, ny) // 6))]
+    a = gpu_run(nx, ny, p, disks, steps)
+    b = oracle_run(nx, ny, p, disks, steps)
+    for x, y in zip(a, b):
+        assert bits_equal(x, y)
+
+
+def test_grid300_2000_steps_matches_golden_hash():
+    """configuration 0 in full: 300^2, 2000 steps, against hashes made on another machine by the oracle"""
+    g = json.load(open(os.path.join(GOLD, "kgm_grid300.json")))
+    for tag in ("theta0_0", "theta0_02"):
+        phi, t, th = gpu_run(300, 300, g[tag]["params"], g["disks"], g["steps"])
+        assert hashlib.sha256(phi.tobytes()).hexdigest() == g[tag]["sha_phi"]
+        assert hashlib.sha256(t.tobytes()).hexdigest() == g[tag]["sha_T"]
+        assert hashlib.sha256(th.tobytes()).hexdigest() == g[tag]["sha_theta"]
+
+
+def test_reference_defaults_within_noise_floor():
+    """the reference's own FP64 output (C-library atan/sin/cos) vs the GPU: 1e-12 relative max-norm"""
+    fx = np.load(os.path.join(GOLD, "ref64_default_64x48.npz"))
+    p = json.loads(str(fx["params"]))
+    sim = Kobayashi(64, 48, p["dt"], params=p)  # kg_create seeds the reference nucleus
+    for _ in range(20):
+        sim.iUpdate()
+    phi, t, th = sim.fields()
+    assert sim.counters() == (200, 20)
+    sim.close()
+    assert np.abs(phi - fx["phi"]).max() / np.abs(fx["phi"]).max() <= 1e-12
+    assert np.abs(t - fx["T"]).max() / np.abs(fx["T"]).max() <= 1e-12
+
+
+@pytest.mark.parametrize("variant", [0, 13, 26, 40, 53])
+def test_variants_2048_truncated(variant):
+    """configuration 2 (anisotropy variants on 2048^2), truncated to 60 steps"""
+    v = configs.variants_2048()[variant]
+    a = gpu_run(v["nx"], v["ny"], v["params"], v["disks"], 60)
+    b = oracle_run(v["nx"], v["ny"], v["params"], v["disks"], 60)
+    for x, y in zip(a, b):
+        assert bits_equal(x, y)
+
+
+def test_grid8192_truncated():
+    """configuration 1 (8192^2, 64 disks), truncated to 12 steps (graph chunk 5 + remainder)"""
+    cfg = configs.grid_8192()
+    a = gpu_run(cfg["nx"], cfg["ny"], cfg["params"], cfg["disks"], 12, chunk=5)
+    b = oracle_run(cfg["nx"], cfg["ny"], cfg["params"], cfg["disks"], 12)
+    for x, y in zip(a, b):
+        assert bits_equal(x, y)
+
+
+def test_graph_chunks_do_not_change_results():
+    p = dict(configs.BASE)
+    disks = [(40, 30, 4)]
+    runs = [gpu_run(80, 60, p, disks, 230, chunk=c) for c in (0, 1, 7, 100)]
+    for r in runs[1:]:
+        for x, y in zip(runs[0], r):
+            assert bits_equal(x, y)
+
+
+def test_translation_invariance_full_size():
+    """periodic grid: shifting the nuclei shifts the solution exactly (every cell runs the same arithmetic)"""
+    cfg = configs.grid_8192()
+    n = cfg["nx"]
+    di, dj = 1234, 567
+    shifted = [((x + di) % n, (y + dj) % n, r) for x, y, r in cfg["disks"]]
+    a = gpu_run(n, n, cfg["params"], cfg["disks"], 30)
+    b = gpu_run(n, n, cfg["params"], shifted, 30)
+    for x, y in zip(a, b):
+        assert bits_equal(np.roll(x, (dj, di), axis=(0, 1)), y)
+
+
+def test_determinism():
+    p = dict(configs.BASE)
+    a = gpu_run(512, 512, p, [(256, 256, 5)], 300)
+    b = gpu_run(512, 512, p, [(256, 256, 5)], 300)
+    for x, y in zip(a, b):
+        assert bits_equal(x, y)
+
+
+def test_set_params_mid_run_and_reset():
+    p = dict(configs.BASE)
+    q = dict(p, delta=0.05, K=1.2, theta0=0.7)
+    sim = Kobayashi(96, 80, p["dt"], params=p)
+    sim.seed_disks([(48, 40, 6)])
+    sim.step(150)
+    sim.set_params(**{k: q[k] for k in ("delta", "K", "theta0")})
+    sim.step(150)
+    got = sim.fields()
+    init = configs.initial_fields(96, 80, [(48, 40, 6)])
+    mid = ko_oracle.port_run(*init, p, 150)
+    ref = ko_oracle.port_run(*mid, q, 150)
+    for x, y in zip(got, ref):
+        assert bits_equal(x, y)
+    sim.iResetSimulationState()
+    phi, t, th = sim.fields()
+    p0, _, _ = configs.initial_fields(96, 80, [(48, 40, 1)])
+    assert bits_equal(phi, p0) and not t.any() and not th.any()
+    assert sim.counters() == (0, 0)
+    sim.close()
+
+
+def test_set_fields_roundtrip_and_continue():
+    p = dict(configs.BASE)
+    rng = np.random.default_rng(5)
+    phi = rng.uniform(0, 1, (50, 70))
+    t = rng.normal(0, 0.1, (50, 70))
+    th = rng.uniform(-1.5, 6.2, (50, 70))
+    sim = Kobayashi(70, 50, p["dt"], params=p)
+    sim.set_fields(phi, t, th)
+    got = sim.fields()
+    for x, y in zip(got, (phi, t, th)):
+        assert bits_equal(x, y)
+    sim.step(40)
+    a = sim.fields()
+    b = ko_oracle.port_run(phi, t, th, p, 40)
+    for x, y in zip(a, b):
+        assert bits_equal(x, y)
+    sim.close()
+
+
+def test_invalid_arguments_fail_cleanly():
+    with pytest.raises(KgError):
+        Kobayashi(0, 10, 1e-4)
+    with pytest.raises(KgError):
+        Kobayashi(10, 10, 1e-4, params=dict(tau=0.0))
+    with pytest.raises(KgError):
+        Kobayashi(10, 10, 1e-4, params=dict(aniso=2.5))
+    sim = Kobayashi(10, 10, 1e-4)
+    with pytest.raises(KgError):
+        sim.step(-1)
+    with pytest.raises(KgError):
+        sim.set_params(dx=float("nan"))
+    sim.step(3)  # still usable
+    sim.close()
