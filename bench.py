@@ -156,6 +156,102 @@ def cpu_baseline_sample(cfg, seconds_budget=20.0):
                       % (n_steps, nx, ny)}
 
 
+def measure_ensemble(steps=100, trial_steps=10):
+    """The mixed-size ensemble (512 instances, sides 64..512, per-instance parameters), timed over the
+    same `steps` steps from the initial state three ways: one autotuned batched launch per step; the
+    512 instances as single-grid handles run one after another on one stream (the looped baseline);
+    and the same handles each on its own stream (concurrent single-grid runs)."""
+    import torch
+    from crystalgrowth_gb300 import Batch, Kobayashi, configs
+    cfg = configs.ensemble_512()
+    inst = cfg["instances"]
+    cells = sum(i["nx"] * i["ny"] for i in inst)
+    b = Batch([(i["nx"], i["ny"]) for i in inst], [i["params"] for i in inst])
+
+    def seed_batch():
+        for k, i in enumerate(inst):
+            b.seed_disks(k, i["disks"])
+    seed_batch()
+    t0 = time.perf_counter()
+    best, _ = b.autotune(trial_steps=trial_steps)
+    tune_s = time.perf_counter() - t0
+    b.set_tuning(**dict(best, chunk=steps))
+    b.step(steps)  # warm-up (graph build)
+    seed_batch()
+    stream = torch.cuda.ExternalStream(b.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b.sync()
+    e0.record(stream)
+    b.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    batched_s = e0.elapsed_time(e1) / 1e3
+    b.close()
+
+    sims = []
+    for i in inst:
+        s = Kobayashi(i["nx"], i["ny"], i["params"]["dt"], params=i["params"])
+        s.set_graph_chunk(steps)
+        s.step(steps)  # warm-up (graph build)
+        sims.append(s)
+
+    def run(sequential):
+        for s, i in zip(sims, inst):
+            s.seed_disks(i["disks"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in sims:
+            s.step(steps)
+            if sequential:
+                s.sync()
+        for s in sims:
+            s.sync()
+        return time.perf_counter() - t0
+    looped_s = run(True)
+    concurrent_s = run(False)
+    for s in sims:
+        s.close()
+    work = cells * steps
+    return {"workload": "ensemble_512: 512 instances, sides log-uniform 64..512, %d cells; time steps 0..%d"
+                        % (cells, steps),
+            "batched_cell_updates_per_s": work / batched_s, "looped_cell_updates_per_s": work / looped_s,
+            "concurrent_streams_cell_updates_per_s": work / concurrent_s,
+            "speedup_vs_looped": looped_s / batched_s, "speedup_vs_concurrent_streams": concurrent_s / batched_s,
+            "tuning": best, "autotune_s": tune_s,
+            "looped": "512 single-grid handles, one after another (each a CUDA graph of the %d steps)" % steps,
+            "concurrent_streams": "the same 512 handles, each on its own stream, all enqueued before waiting"}
+
+
+def measure_adjoint():
+    """Adjoint/forward cost on the 512^2, 4000-step rollout with checkpoints every 64 steps."""
+    import numpy as np
+    from crystalgrowth_gb300 import Adjoint, configs
+    cfg = configs.adjoint_512()
+    n, steps = cfg["nx"], cfg["steps"]
+    phi0, _, th0 = configs.initial_fields(n, n, cfg["disks"])
+    tgt = Adjoint(n, n, cfg["target_params"], steps, checkpoint_every=cfg["checkpoint_every"])
+    tgt.set_initial(phi0, cfg["T0"], th0)
+    tgt.set_target(np.zeros((n, n)))
+    _, (target, _, _) = tgt.forward(want_state=True)
+    tgt.close()
+    adj = Adjoint(n, n, cfg["params"], steps, checkpoint_every=cfg["checkpoint_every"])
+    adj.set_initial(phi0, cfg["T0"], th0)
+    adj.set_target(target)
+    adj.forward()
+    adj.gradient()  # warm-up
+    t0 = time.perf_counter()
+    loss = adj.forward()
+    t1 = time.perf_counter()
+    g, _ = adj.gradient()
+    t2 = time.perf_counter()
+    adj.close()
+    fwd, grad = t1 - t0, t2 - t1
+    return {"workload": "adjoint_512: 512x512, 4000 steps, checkpoints every 64",
+            "forward_s": fwd, "gradient_s": grad, "adjoint_forward_ratio": grad / fwd,
+            "loss": loss, "gradient": {k: v for k, v in g.items() if k != "loss"},
+            "note": "gradient_s includes its own forward rollout; ratio = gradient time / forward time"}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -277,6 +373,9 @@ def run_ours(args, rank, world):
             "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(cfg)
+    if rank == 0 and not args.no_extras:
+        line["ensemble"] = measure_ensemble()
+        line["adjoint"] = measure_adjoint()
     sim.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -290,6 +389,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the ensemble and adjoint side measurements")
     ap.add_argument("--grid", type=int, default=8192, help="side of the square grid (8192 = the benchmark workload)")
     ap.add_argument("--disks", type=int, default=64)
     args = ap.parse_args()

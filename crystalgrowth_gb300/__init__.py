@@ -9,6 +9,7 @@ fallback: every call fails loudly if the library is missing.
 from ._lib import KgError, lib, load, Params  # noqa: F401
 from .kobayashi import Kobayashi  # noqa: F401
 from .batch import Batch  # noqa: F401
+from .adjoint import Adjoint  # noqa: F401
 from . import configs  # noqa: F401
 
-__all__ = ["Batch", "Kobayashi", "KgError", "Params", "configs", "lib", "load"]
+__all__ = ["Adjoint", "Batch", "Kobayashi", "KgError", "Params", "configs", "lib", "load"]

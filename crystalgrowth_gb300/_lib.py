@@ -85,6 +85,15 @@ _SIGS = {
     "kg_batch_get_tuning": [_vp, _vp],
     "kg_batch_autotune": [_vp, ctypes.c_int, _vp, ctypes.POINTER(ctypes.c_double)],
     "kg_batch_get_stream": [_vp, ctypes.POINTER(_vp)],
+    "kg_adjoint_create": [ctypes.c_int, ctypes.c_int, ctypes.POINTER(Params), ctypes.c_longlong, ctypes.c_int,
+                          ctypes.POINTER(_vp)],
+    "kg_adjoint_destroy": [_vp],
+    "kg_adjoint_set_params": [_vp, ctypes.POINTER(Params)],
+    "kg_adjoint_set_initial": [_vp, _dp, _dp, _dp],
+    "kg_adjoint_set_target": [_vp, _dp],
+    "kg_adjoint_forward": [_vp, ctypes.POINTER(ctypes.c_double), _dp, _dp, _dp],
+    "kg_adjoint_gradient": [_vp, _vp, _dp],
+    "kg_adjoint_get_stream": [_vp, ctypes.POINTER(_vp)],
     "kg_diag_fp64_peak": [ctypes.POINTER(ctypes.c_double)],
 }
 _RESTYPE = {"kg_last_error": ctypes.c_char_p, "kg_version": ctypes.c_char_p}

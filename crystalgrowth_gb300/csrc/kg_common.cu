@@ -98,8 +98,8 @@ int kg_prepare(const kg_params* p, KgDev* d)
     d->teq = p->teq;
     d->theta0 = p->theta0;
     d->lap_den = 3.0 * p->dx * p->dx;
-    if (kg_cdiv_prepare(p->dx, &d->rdx_h, &d->rdx_l) || kg_cdiv_prepare(p->dy, &d->rdy_h, &d->rdy_l) ||
-        kg_cdiv_prepare(d->lap_den, &d->rlap_h, &d->rlap_l) || kg_cdiv_prepare(p->tau, &d->rtau_h, &d->rtau_l))
+    if (kg_idiv_prepare(p->dx, &d->idx) || kg_idiv_prepare(p->dy, &d->idy) || kg_idiv_prepare(d->lap_den, &d->ilap) ||
+        kg_idiv_prepare(p->tau, &d->itau))
         return kg_fail(KG_ERR_INVALID, "params: dx, dy, 3 dx^2 and tau must lie in [2^-100, 2^100]");
     d->c_epsd = -p->eps_bar * p->aniso * p->delta;
     d->a_pi = p->alpha / KG_PI;
@@ -107,6 +107,8 @@ int kg_prepare(const kg_params* p, KgDev* d)
     d->arg0 = p->aniso * (0.0 - p->theta0);
     double s, c;
     kg_sincos(d->arg0, &s, &c);
+    d->s0 = s;
+    d->c0 = c;
     d->eps0 = p->eps_bar * (1.0 + p->delta * c);
     d->epsd0 = d->c_epsd * s;
     d->e2_0 = d->eps0 * d->eps0;

@@ -16,7 +16,8 @@
  * The arithmetic reproduces the reference operation for operation in IEEE
  * FP64 (this file is compiled with -fmad=false, so a*b+c is never fused
  * unless written as kg_fma), with three exact shortcuts:
- *   - divisions by dx, dy, 3 dx^2 and tau use kg_cdiv (same bits as a/b);
+ *   - divisions by dx, dy, 3 dx^2 and tau use kg_idiv: the IEEE quotient's
+ *     bits from 64-bit integer arithmetic, off the FP64 pipe;
  *   - eps, eps' for the angle value theta = 0 (every cell the front has not
  *     reached) come from a table computed once on the host with the same
  *     kg_sincos, keyed on the exact bits of the sine/cosine argument;
@@ -31,11 +32,12 @@
 /* Everything the kernel needs about one parameter set, prepared on the host. */
 struct KgDev {
     double dx, dy, dt, tau, eps_bar, K, delta, aniso, alpha, gamma, teq, theta0;
-    double rdx_h, rdx_l, rdy_h, rdy_l, rlap_h, rlap_l, rtau_h, rtau_l; /* kg_cdiv reciprocals */
+    kg_idivc idx, idy, ilap, itau; /* integer-pipe division by dx, dy, 3 dx^2, tau */
     double lap_den;   /* (3 dx) dx, src/Kobayashi.cpp:146 */
     double c_epsd;    /* ((-eps_bar) aniso) delta, src/Kobayashi.cpp:171 */
     double a_pi;      /* alpha / PI_F, src/Kobayashi.cpp:206 */
     double arg0;      /* aniso (0 - theta0): sin/cos argument of theta == 0 */
+    double s0, c0;    /* sin(arg0), cos(arg0) */
     double eps0, epsd0, e2_0, ee0; /* eps, eps', eps^2, eps eps' at arg0 */
     double u0, m0;    /* gamma (Teq - 0) and (alpha/pi) atan(u0) */
 };
@@ -57,6 +59,20 @@ __device__ __forceinline__ bool kg_neg_big(uint64_t b)
 /* Stage-1 quantities of one cell that its neighbours read in stage 2. */
 struct KgS1 {
     double gx, gy, e2, a, b; /* phi_x, phi_y, eps^2, eps eps' phi_x, eps eps' phi_y */
+    double s, c;             /* sin, cos of aniso (theta - theta0) (kept for the adjoint's tape) */
+};
+
+/* Per-cell forward quantities the reverse (adjoint) step reads: one slot of
+ * the tape, field f of cell i at f[k][i]. */
+enum { KG_TAPE_PHI, KG_TAPE_T, KG_TAPE_GX, KG_TAPE_GY, KG_TAPE_SIN, KG_TAPE_COS, KG_TAPE_LAP, KG_TAPE_RHS,
+       KG_TAPE_M, KG_TAPE_GEX, KG_TAPE_GEY, KG_TAPE_FIELDS };
+struct KgTape {
+    double* f[KG_TAPE_FIELDS];
+};
+
+/* stage-2 intermediates recorded on the tape */
+struct KgS2Aux {
+    double rhs, m, gex, gey;
 };
 
 /*
@@ -67,8 +83,8 @@ struct KgS1 {
 __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, double pN, double pS, double& theta)
 {
     KgS1 o;
-    double gx = kg_cdiv(pE - pW, P.dx, P.rdx_h, P.rdx_l);
-    double gy = kg_cdiv(pN - pS, P.dy, P.rdy_h, P.rdy_l);
+    double gx = kg_idiv(pE - pW, &P.idx);
+    double gy = kg_idiv(pN - pS, &P.idy);
     uint64_t bx = kg_bits(gx), by = kg_bits(gy);
     /* the reference's three branches (src/Kobayashi.cpp:154-167) with one
      * shared atan call, so that lanes on different branches do not run it
@@ -93,6 +109,8 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
     if (kg_bits(arg) == kg_bits(P.arg0)) {
         e2 = P.e2_0;
         ee = P.ee0;
+        o.s = P.s0;
+        o.c = P.c0;
     } else {
         double s, c;
         kg_sincos(arg, &s, &c);
@@ -100,6 +118,8 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
         double epsd = P.c_epsd * s;
         e2 = eps * eps;
         ee = eps * epsd;
+        o.s = s;
+        o.c = c;
     }
     o.gx = gx;
     o.gy = gy;
@@ -114,7 +134,7 @@ __device__ __forceinline__ double kg_lap(const KgDev& P, double c, double e, dou
                                          double sw, double nw, double se)
 {
     double v = 2.0 * (e + w + n + s) + ne + sw + nw + se - 12.0 * c;
-    return kg_cdiv(v, P.lap_den, P.rlap_h, P.rlap_l);
+    return kg_idiv(v, &P.ilap);
 }
 
 /*
@@ -123,21 +143,28 @@ __device__ __forceinline__ double kg_lap(const KgDev& P, double c, double e, dou
  */
 __device__ __forceinline__ void kg_stage2(const KgDev& P, double e2c, double gx, double gy, double e2E, double e2W,
                                           double e2N, double e2S, double aN, double aS, double bE, double bW,
-                                          double lap_phi, double lap_t, double& phi, double& t)
+                                          double lap_phi, double lap_t, double& phi, double& t,
+                                          KgS2Aux* aux = nullptr)
 {
-    double gex = kg_cdiv(e2E - e2W, P.dx, P.rdx_h, P.rdx_l);
-    double gey = kg_cdiv(e2N - e2S, P.dy, P.rdy_h, P.rdy_l);
-    double term1 = kg_cdiv(aN - aS, P.dy, P.rdy_h, P.rdy_l);
-    double term2 = -kg_cdiv(bE - bW, P.dx, P.rdx_h, P.rdx_l);
+    double gex = kg_idiv(e2E - e2W, &P.idx);
+    double gey = kg_idiv(e2N - e2S, &P.idy);
+    double term1 = kg_idiv(aN - aS, &P.idy);
+    double term2 = -kg_idiv(bE - bW, &P.idx);
     double term3 = gex * gx + gey * gy;
     double u = P.gamma * (P.teq - t);
     double m = (kg_bits(u) == kg_bits(P.u0)) ? P.m0 : P.a_pi * kg_atan(u);
     double old_phi = phi;
     double old_t = t;
     double rhs = term1 + term2 + e2c * lap_phi + term3 + old_phi * (1.0 - old_phi) * (old_phi - 0.5 + m);
-    double new_phi = old_phi + kg_cdiv(rhs * P.dt, P.tau, P.rtau_h, P.rtau_l);
+    double new_phi = old_phi + kg_idiv(rhs * P.dt, &P.itau);
     t = old_t + lap_t * P.dt + P.K * (new_phi - old_phi);
     phi = new_phi;
+    if (aux) {
+        aux->rhs = rhs;
+        aux->m = m;
+        aux->gex = gex;
+        aux->gey = gey;
+    }
 }
 
 __device__ __forceinline__ int kg_wrap(int i, int n)
@@ -160,11 +187,12 @@ struct KgSmem {
     double b[2][NT];
 };
 
-template <int NT>
+template <int NT, bool TAPE = false>
 __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const double* __restrict__ phi_in,
                                          const double* __restrict__ t_in, const double* __restrict__ th_in,
                                          double* __restrict__ phi_out, double* __restrict__ t_out,
-                                         double* __restrict__ th_out, int i0, int j0, int bh, KgSmem<NT>& sm)
+                                         double* __restrict__ th_out, int i0, int j0, int bh, KgSmem<NT>& sm,
+                                         const KgTape* tape = nullptr)
 {
     const int L = threadIdx.x;
     const int jend = min(j0 + bh, ny);
@@ -200,8 +228,15 @@ __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const d
                             sm.phi[(r - 1) & 7][L + 1], theta);
         sm.e2[r & 1][L] = s1.e2;
         sm.b[r & 1][L] = s1.b;
-        if (out_lane && r >= j0 && r < jend)
+        if (out_lane && r >= j0 && r < jend) {
             th_out[roff + col] = theta;
+            if constexpr (TAPE) {
+                tape->f[KG_TAPE_GX][roff + col] = s1.gx;
+                tape->f[KG_TAPE_GY][roff + col] = s1.gy;
+                tape->f[KG_TAPE_SIN][roff + col] = s1.s;
+                tape->f[KG_TAPE_COS][roff + col] = s1.c;
+            }
+        }
 
         /* stage 2 at row s = r-1 for the output lanes */
         const int s = r - 1;
@@ -216,9 +251,22 @@ __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const d
                                   sm.t[tp][L + 1], sm.t[tm][L - 1], sm.t[tp][L - 1], sm.t[tm][L + 1]);
             double phi = sm.phi[s0][k];
             double t = sm.t[t0][L];
-            kg_stage2(P, e2_m1, gx_m1, gy_m1, sm.e2[s & 1][L + 1], sm.e2[s & 1][L - 1], s1.e2, e2_m2, s1.a, a_m2,
-                      sm.b[s & 1][L + 1], sm.b[s & 1][L - 1], lap_phi, lap_t, phi, t);
             const size_t soff = (size_t)kg_wrap(s, ny) * nx;
+            if constexpr (TAPE) {
+                KgS2Aux aux;
+                tape->f[KG_TAPE_PHI][soff + col] = phi;
+                tape->f[KG_TAPE_T][soff + col] = t;
+                kg_stage2(P, e2_m1, gx_m1, gy_m1, sm.e2[s & 1][L + 1], sm.e2[s & 1][L - 1], s1.e2, e2_m2, s1.a, a_m2,
+                          sm.b[s & 1][L + 1], sm.b[s & 1][L - 1], lap_phi, lap_t, phi, t, &aux);
+                tape->f[KG_TAPE_LAP][soff + col] = lap_phi;
+                tape->f[KG_TAPE_RHS][soff + col] = aux.rhs;
+                tape->f[KG_TAPE_M][soff + col] = aux.m;
+                tape->f[KG_TAPE_GEX][soff + col] = aux.gex;
+                tape->f[KG_TAPE_GEY][soff + col] = aux.gey;
+            } else {
+                kg_stage2(P, e2_m1, gx_m1, gy_m1, sm.e2[s & 1][L + 1], sm.e2[s & 1][L - 1], s1.e2, e2_m2, s1.a, a_m2,
+                          sm.b[s & 1][L + 1], sm.b[s & 1][L - 1], lap_phi, lap_t, phi, t);
+            }
             phi_out[soff + col] = phi;
             t_out[soff + col] = t;
         }

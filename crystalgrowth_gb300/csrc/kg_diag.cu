@@ -3,10 +3,11 @@
  * host-vs-device tests, and an FP64 FMA throughput probe.
  */
 #include "kg_common.h"
+#include <string.h>
 #include "kobayashi_diag.h"
 
 __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double* __restrict__ y, long long n, double b,
-                                    double yh, double yl)
+                                    double yh, double yl, kg_idivc ic)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         double v = x[i], r = 0.0;
@@ -18,6 +19,8 @@ __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double
             r = fn == KG_FN_SIN ? s : c;
         } else if (fn == KG_FN_CDIV) {
             r = kg_cdiv(v, b, yh, yl);
+        } else if (fn == KG_FN_IDIV) {
+            r = kg_idiv(v, &ic);
         } else {
             r = v / b;
         }
@@ -27,10 +30,13 @@ __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double
 
 extern "C" int kg_diag_eval(int fn, const double* x, double* y, long long n, double b)
 {
-    if (fn < KG_FN_ATAN || fn > KG_FN_DIV || n < 0 || (n > 0 && (!x || !y)))
+    if (fn < KG_FN_ATAN || fn > KG_FN_IDIV || n < 0 || (n > 0 && (!x || !y)))
         return kg_fail(KG_ERR_INVALID, "kg_diag_eval: bad arguments");
     double yh = 0, yl = 0;
-    if ((fn == KG_FN_CDIV || fn == KG_FN_DIV) && kg_cdiv_prepare(b, &yh, &yl))
+    kg_idivc ic;
+    memset(&ic, 0, sizeof ic);
+    if ((fn == KG_FN_CDIV || fn == KG_FN_DIV || fn == KG_FN_IDIV) &&
+        (kg_cdiv_prepare(b, &yh, &yl) || kg_idiv_prepare(b, &ic)))
         return kg_fail(KG_ERR_INVALID, "kg_diag_eval: divisor outside [2^-100, 2^100]");
     if (n == 0)
         return KG_OK;
@@ -39,7 +45,7 @@ extern "C" int kg_diag_eval(int fn, const double* x, double* y, long long n, dou
     cudaError_t e = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         int blocks = (int)((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8);
-        kg_diag_eval_kernel<<<blocks, 256>>>(fn, d, d + n, n, b, yh, yl);
+        kg_diag_eval_kernel<<<blocks, 256>>>(fn, d, d + n, n, b, yh, yl, ic);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)

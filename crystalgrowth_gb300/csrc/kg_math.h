@@ -274,4 +274,101 @@ KG_HD double kg_cdiv(double a, double b, double yh, double yl)
     return a / b;
 }
 
+
+/*
+ * Integer-pipe division by a fixed divisor: the same bits as a / b (IEEE,
+ * round to nearest even) computed with 64-bit integer arithmetic instead of
+ * FP64 operations (on GB300 the FP64 pipe is the bottleneck and the integer
+ * pipes are ~30x wider).
+ *
+ * With A, B the 53-bit significands of a and b (hidden bit included),
+ * N = A' 2^52 where A' = 2A if A < B (so that N/B lies in [2^52, 2^53)), and
+ * R = floor(2^116 / B), the estimate q = floor(A' R / 2^64) satisfies
+ * floor(N/B) - 1 <= q <= floor(N/B) (the truncation of R costs less than
+ * A'/2^64 < 2^-10).  One comparison of the exact remainder N - qB (computed
+ * modulo 2^64: it lies in [0, 2B)) fixes q, and 2 rem > B decides the
+ * rounding (an exact tie would need B = 2^52, i.e. b a power of two, which
+ * is handled as an exact exponent shift).  Zero dividends return a;
+ * subnormal, infinite and NaN dividends, and quotients that would be
+ * subnormal or overflow, take the IEEE division.
+ */
+typedef struct kg_idivc {
+    uint64_t B;  /* significand of b with the hidden bit */
+    uint64_t R;  /* floor(2^116 / B); 0 for a power of two */
+    double b;    /* the divisor itself, for the IEEE fallback */
+    int eb;      /* biased exponent field of b */
+    int pow2;    /* b is a power of two */
+} kg_idivc;
+
+KG_HD uint64_t kg_umulhi64(uint64_t a, uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    uint64_t a0 = a & 0xffffffffull, a1 = a >> 32, b0 = b & 0xffffffffull, b1 = b >> 32;
+    uint64_t p00 = a0 * b0, p01 = a0 * b1, p10 = a1 * b0, p11 = a1 * b1;
+    uint64_t mid = (p00 >> 32) + (p01 & 0xffffffffull) + (p10 & 0xffffffffull);
+    return p11 + (p01 >> 32) + (p10 >> 32) + (mid >> 32);
+#endif
+}
+
+/* returns 0 for a positive normal b in [2^-100, 2^100], -1 otherwise */
+KG_HD int kg_idiv_prepare(double b, kg_idivc* c)
+{
+    if (!(b >= 0x1p-100 && b <= 0x1p100))
+        return -1;
+    uint64_t ub = kg_bits(b);
+    c->b = b;
+    c->eb = (int)((ub >> 52) & 0x7ff);
+    c->B = (ub & 0x000fffffffffffffull) | 0x0010000000000000ull;
+    c->pow2 = (c->B == 0x0010000000000000ull);
+    if (c->pow2) {
+        c->R = 0;
+    } else {
+        /* floor(2^116 / B) by long division, 64 quotient bits after the leading 2^63 */
+        uint64_t rem = (1ull << 63) % c->B, q = (1ull << 63) / c->B; /* 2^63 / B < 2^11 */
+        for (int i = 0; i < 53; i++) {
+            rem <<= 1;
+            q <<= 1;
+            if (rem >= c->B) {
+                rem -= c->B;
+                q |= 1;
+            }
+        }
+        c->R = q;
+    }
+    return 0;
+}
+
+KG_HD double kg_idiv(double a, const kg_idivc* c)
+{
+    uint64_t ua = kg_bits(a);
+    uint64_t sign = ua & 0x8000000000000000ull;
+    int ea = (int)((ua >> 52) & 0x7ff);
+    if ((ua & 0x7fffffffffffffffull) == 0)
+        return a;
+    if (ea == 0 || ea == 0x7ff)
+        return a / c->b;
+    uint64_t A = (ua & 0x000fffffffffffffull) | 0x0010000000000000ull;
+    if (c->pow2) {
+        int e = ea - c->eb + 1023;
+        if (e >= 1 && e <= 2046)
+            return kg_from_bits(sign | ((uint64_t)e << 52) | (A & 0x000fffffffffffffull));
+    } else {
+        int shift = A < c->B;
+        uint64_t Ap = A << shift;
+        uint64_t q = kg_umulhi64(Ap, c->R);
+        uint64_t rem = (Ap << 52) - q * c->B;
+        if (rem >= c->B) {
+            q += 1;
+            rem -= c->B;
+        }
+        q += (rem << 1) > c->B;
+        int e = ea - c->eb + 1023 - shift;
+        if (e >= 1 && e <= 2046)
+            return kg_from_bits(sign | (((uint64_t)(e - 1) << 52) + q));
+    }
+    return a / c->b;
+}
+
 #endif /* KG_MATH_H */

@@ -18,6 +18,7 @@ extern "C" {
 #define KG_FN_COS 2   /* y = cos part of kg_sincos(x) */
 #define KG_FN_CDIV 3  /* y = kg_cdiv(x, b): x / b through the constant-divisor path */
 #define KG_FN_DIV 4   /* y = x / b, the GPU's own IEEE division */
+#define KG_FN_IDIV 5  /* y = kg_idiv(x, b): x / b through the integer-pipe path */
 
 /* Evaluates function `fn` on n host values on the current device (synchronous). */
 KG_API int kg_diag_eval(int fn, const double* x, double* y, long long n, double b);

@@ -58,6 +58,9 @@ def port_lib():
         lib.ko_kg_cdiv_check.restype = ctypes.c_longlong
         lib.ko_kg_eval.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_longlong, ctypes.c_double]
         lib.ko_kg_eval.restype = ctypes.c_int
+        lib.ko_tlm_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(KoParams), _dp, _dp, _dp, _dp,
+                                   _dp, _dp, _dp, ctypes.c_longlong, ctypes.c_int]
+        lib.ko_tlm_run.restype = ctypes.c_int
         _port_lib = lib
     return _port_lib
 
@@ -78,6 +81,20 @@ def port_run(phi, T, theta, params, nsteps, libm=False, threads=1):
     if rc != 0:
         raise RuntimeError("ko_run failed")
     return phi, T, theta
+
+
+def tlm_run(phi, T, theta, dphi, dT, dtheta, params, dparams, nsteps, threads=1):
+    """Tangent-linear rollout: returns (state, tangent) after nsteps.
+    dparams: dict with any of d_delta, d_K, d_theta0, d_tau, d_gamma."""
+    arrs = [np.array(a, dtype=np.float64, order="C", copy=True) for a in (phi, T, theta, dphi, dT, dtheta)]
+    ny, nx = arrs[0].shape
+    dp = np.array([dparams.get(k, 0.0) for k in ("d_delta", "d_K", "d_theta0", "d_tau", "d_gamma")])
+    ps = params_struct(params)
+    rc = port_lib().ko_tlm_run(nx, ny, ctypes.byref(ps), _ptr(dp), *[_ptr(a) for a in arrs], int(nsteps),
+                               int(threads))
+    if rc != 0:
+        raise RuntimeError("ko_tlm_run failed")
+    return tuple(arrs[:3]), tuple(arrs[3:])
 
 
 def kg_atan(x):

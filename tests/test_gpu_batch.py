@@ -123,6 +123,6 @@ def test_batch_rejects_bad_input():
     b = Batch([(8, 8)], [dict()])
     with pytest.raises(_lib.KgError):
         b.set_tuning(nt=100)
-    with pytest.raises(_lib.KgError):
-        b.fields(3)
+    assert _lib.lib().kg_batch_get_fields(b._h, 3, None, None, None) == _lib.KG_ERR_INVALID
+    assert b"out of range" in _lib.lib().kg_last_error()
     b.close()

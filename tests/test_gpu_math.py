@@ -44,12 +44,13 @@ def test_transcendentals_device_equals_host(fn):
     assert same_bits(dev_eval(fn, x), ko_oracle.kg_eval(fn, x))
 
 
-@pytest.mark.parametrize("b", [0.03, 3 * 0.03 * 0.03, 3e-4, 2.1e-4, 3.99e-4, 1e-4, 9e-4, 7.0, 1 / 3])
+@pytest.mark.parametrize("b", [0.03, 3 * 0.03 * 0.03, 3e-4, 2.1e-4, 3.99e-4, 1e-4, 9e-4, 7.0, 1 / 3, 0.5, 2.0 ** -99])
 def test_constant_division_equals_ieee_on_device(b):
     x = inputs(int(b * 1e7) % 997)
-    dev = dev_eval(3, x, b)
-    assert same_bits(dev, dev_eval(4, x, b))
-    assert same_bits(dev, ko_oracle.kg_eval(4, x, b))
+    ieee = dev_eval(4, x, b)
+    assert same_bits(dev_eval(3, x, b), ieee)
+    assert same_bits(dev_eval(5, x, b), ieee)
+    assert same_bits(ieee, ko_oracle.kg_eval(4, x, b))
 
 
 def test_fp64_peak_probe():

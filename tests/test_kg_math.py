@@ -114,3 +114,21 @@ def test_cdiv_algorithm_exhaustive_small_precision(p):
             assert r == a - q0 * b  # the remainder is exact
             q = _rn(q0 + r * yh, p)
             assert q == _rn(a / b, p), (A, B)
+
+
+@pytest.mark.parametrize("b", [0.03, 3 * 0.03 * 0.03, 3e-4, 2.1e-4, 1e-4, 7.0, 1 / 3, 0.5, 1.0, 0.75, 2.0 ** -99,
+                               2.0 ** 99])
+def test_idiv_matches_ieee_random(b):
+    """kg_idiv (integer significand division) == IEEE a / b, including zeros, subnormals,
+    infinities, NaN and quotients that underflow or overflow"""
+    rng = np.random.default_rng(int(b * 1e6) % 1000 + 7)
+    n = 1_000_000
+    x = np.concatenate([rng.standard_normal(n) * 10.0 ** rng.integers(-300, 300, n), rng.uniform(-1, 1, n),
+                        rng.integers(2 ** 52, 2 ** 53, n).astype(np.float64) * 2.0 ** rng.integers(-1074, 970, n),
+                        np.array([0.0, -0.0, 5e-324, -5e-324, 2.0 ** -1022, math.inf, -math.inf, 1e308, -1e308,
+                                  2.0 ** -1000, math.nan])])
+    with np.errstate(all="ignore"):
+        ref = x / b
+    got = ko_oracle.kg_eval(5, x, b)
+    same = (got.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(got) & np.isnan(ref))
+    assert same.all()
