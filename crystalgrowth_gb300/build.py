@@ -29,7 +29,8 @@ def nvcc():
 
 
 def cflags():
-    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
+    extra = os.environ.get("KG_NVCC_EXTRA", "").split()
+    return ARCH + extra + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
                    "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
                    "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 

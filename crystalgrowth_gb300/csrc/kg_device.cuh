@@ -129,11 +129,30 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
     return o;
 }
 
+/*
+ * How much of the step's FP64 arithmetic moves to the integer pipes
+ * (bit-identical either way, see kg_math.h):
+ *   0  the FP64 pipe does every add and multiply
+ *   1  the Laplacians' doubling 2 (E+W+N+S) is an exponent increment
+ *   2  as 1, and the Laplacians' eight neighbour additions use kg_iadd
+ */
+#ifndef KG_EMU
+#define KG_EMU 0
+#endif
+
 /* 9-point Laplacian in the reference's summation order (src/Kobayashi.cpp:142-151). */
 __device__ __forceinline__ double kg_lap(const KgDev& P, double c, double e, double w, double n, double s, double ne,
                                          double sw, double nw, double se)
 {
-    double v = 2.0 * (e + w + n + s) + ne + sw + nw + se - 12.0 * c;
+    double v;
+#if KG_EMU >= 2
+    double s4 = kg_iadd(kg_iadd(kg_iadd(e, w), n), s);
+    v = kg_iadd(kg_iadd(kg_iadd(kg_iadd(kg_imul2(s4), ne), sw), nw), se) - 12.0 * c;
+#elif KG_EMU == 1
+    v = kg_imul2(e + w + n + s) + ne + sw + nw + se - 12.0 * c;
+#else
+    v = 2.0 * (e + w + n + s) + ne + sw + nw + se - 12.0 * c;
+#endif
     return kg_idiv(v, &P.ilap);
 }
 

@@ -21,7 +21,15 @@ __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double
             r = kg_cdiv(v, b, yh, yl);
         } else if (fn == KG_FN_IDIV) {
             r = kg_idiv(v, &ic);
-        } else {
+        } else if (fn == KG_FN_IADD) {
+            r = kg_iadd(v, x[n - 1 - i]);
+        } else if (fn == KG_FN_ADD) {
+            r = __dadd_rn(v, x[n - 1 - i]);
+        } else if (fn == KG_FN_IMUL2) {
+            r = kg_imul2(v);
+        } else if (fn == KG_FN_MUL2) {
+            r = __dmul_rn(2.0, v);
+        } else if (fn == KG_FN_DIV) {
             r = v / b;
         }
         y[i] = r;
@@ -30,7 +38,7 @@ __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double
 
 extern "C" int kg_diag_eval(int fn, const double* x, double* y, long long n, double b)
 {
-    if (fn < KG_FN_ATAN || fn > KG_FN_IDIV || n < 0 || (n > 0 && (!x || !y)))
+    if (fn < KG_FN_ATAN || fn > KG_FN_MUL2 || n < 0 || (n > 0 && (!x || !y)))
         return kg_fail(KG_ERR_INVALID, "kg_diag_eval: bad arguments");
     double yh = 0, yl = 0;
     kg_idivc ic;

@@ -371,4 +371,84 @@ KG_HD double kg_idiv(double a, const kg_idivc* c)
     return a / c->b;
 }
 
+
+KG_HD int kg_clz64(uint64_t x)
+{
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)x);
+#else
+    return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+/*
+ * a + b (IEEE binary64, round to nearest even) in 64-bit integer arithmetic,
+ * the same bits as the hardware addition; infinite and NaN operands take the
+ * hardware path.  Significands carry 10 guard bits (hidden bit at bit 62);
+ * bits shifted out of the smaller operand fold into a sticky bit; an exact
+ * cancellation gives +0; results below 2^-1022 stay exact (subnormal).
+ */
+KG_HD double kg_iadd(double a, double b)
+{
+    uint64_t ua = kg_bits(a), ub = kg_bits(b);
+    uint64_t aa = ua & 0x7fffffffffffffffull, ab = ub & 0x7fffffffffffffffull;
+    if (aa >= 0x7ff0000000000000ull || ab >= 0x7ff0000000000000ull)
+        return a + b;
+    int swap = ab > aa;
+    uint64_t ux = swap ? ub : ua, uy = swap ? ua : ub;
+    uint64_t ax = swap ? ab : aa, ay = swap ? aa : ab;
+    int ex = (int)(ax >> 52), ey = (int)(ay >> 52);
+    uint64_t mx = ((ax & 0x000fffffffffffffull) | (ex ? 0x0010000000000000ull : 0)) << 10;
+    uint64_t my = ((ay & 0x000fffffffffffffull) | (ey ? 0x0010000000000000ull : 0)) << 10;
+    ex += ex == 0;
+    ey += ey == 0;
+    int d = ex - ey;
+    uint64_t myal;
+    if (d >= 64)
+        myal = my != 0;
+    else if (d > 0)
+        myal = (my >> d) | ((my << (64 - d)) != 0);
+    else
+        myal = my;
+    uint64_t sign = ux & 0x8000000000000000ull;
+    int e = ex;
+    uint64_t mm;
+    if (((ux ^ uy) >> 63) == 0) {
+        mm = mx + myal;
+        if (mm >> 63) {
+            mm = (mm >> 1) | (mm & 1);
+            e += 1;
+        }
+    } else {
+        mm = mx - myal;
+        if (mm == 0)
+            return 0.0;
+        int lz = kg_clz64(mm) - 1;
+        if (lz > e - 1)
+            lz = e - 1;
+        mm <<= lz;
+        e -= lz;
+    }
+    if (e >= 2047)
+        return kg_from_bits(sign | 0x7ff0000000000000ull);
+    uint64_t rb = mm & 0x3ff;
+    uint64_t q = mm >> 10;
+    q += (rb > 0x200) | ((rb == 0x200) & (q & 1));
+    return kg_from_bits(sign | (((uint64_t)(e - 1) << 52) + q));
+}
+
+
+/* 2 x, exactly, by an exponent-field increment (subnormals shift their
+ * significand; exponent 2046, infinities and NaN take the hardware path) */
+KG_HD double kg_imul2(double x)
+{
+    uint64_t u = kg_bits(x);
+    uint64_t a = u & 0x7fffffffffffffffull;
+    if (a >= 0x7fe0000000000000ull)
+        return x + x;
+    if (a < 0x0010000000000000ull)
+        return kg_from_bits((u & 0x8000000000000000ull) | (a << 1));
+    return kg_from_bits(u + 0x0010000000000000ull);
+}
+
 #endif /* KG_MATH_H */

@@ -19,6 +19,10 @@ extern "C" {
 #define KG_FN_CDIV 3  /* y = kg_cdiv(x, b): x / b through the constant-divisor path */
 #define KG_FN_DIV 4   /* y = x / b, the GPU's own IEEE division */
 #define KG_FN_IDIV 5  /* y = kg_idiv(x, b): x / b through the integer-pipe path */
+#define KG_FN_IADD 6  /* y[i] = kg_iadd(x[i], x[n-1-i]): integer-pipe addition */
+#define KG_FN_ADD 7   /* y[i] = x[i] + x[n-1-i], the hardware addition */
+#define KG_FN_IMUL2 8 /* y = kg_imul2(x): 2 x by an exponent increment */
+#define KG_FN_MUL2 9  /* y = 2 x, the hardware multiplication */
 
 /* Evaluates function `fn` on n host values on the current device (synchronous). */
 KG_API int kg_diag_eval(int fn, const double* x, double* y, long long n, double b);

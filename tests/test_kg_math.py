@@ -132,3 +132,32 @@ def test_idiv_matches_ieee_random(b):
     got = ko_oracle.kg_eval(5, x, b)
     same = (got.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(got) & np.isnan(ref))
     assert same.all()
+
+
+def _pairs(seed, n=1_000_000):
+    rng = np.random.default_rng(seed)
+    base = rng.standard_normal(n)
+    sub = rng.integers(0, 2 ** 53, n).astype(np.float64) * 5e-324 * rng.choice([-1, 1], n)
+    edge = np.array([0.0, -0.0, 5e-324, -5e-324, 1.7976931348623157e308, 1.7976931348623157e308, -0.0, -0.0,
+                     math.inf, -math.inf, math.nan, 1.0, 2.0 ** -1022, -2.0 ** -1022, 1e308, 1e308])
+    return [rng.standard_normal(n) * 10.0 ** rng.integers(-320, 308, n),
+            np.concatenate([base, -base[::-1] * (1 + rng.integers(-50, 50, n) * 2.0 ** -52)]),
+            np.concatenate([rng.uniform(-1, 1, n), rng.uniform(-1, 1, n) * 2.0 ** rng.integers(-60, 60, n)]),
+            np.concatenate([sub, sub * rng.uniform(0, 3, n)]), edge]
+
+
+def _same(a, r):
+    return bool(((a.view(np.uint64) == r.view(np.uint64)) | (np.isnan(a) & np.isnan(r))).all())
+
+
+def test_iadd_matches_hardware_addition():
+    """kg_iadd(x[i], x[n-1-i]) == x[i] + x[n-1-i]: wide exponents, cancellation, subnormals, overflow"""
+    for x in _pairs(21):
+        with np.errstate(all="ignore"):
+            assert _same(ko_oracle.kg_eval(6, x), ko_oracle.kg_eval(7, x))
+
+
+def test_imul2_matches_hardware():
+    for x in _pairs(22):
+        with np.errstate(all="ignore"):
+            assert _same(ko_oracle.kg_eval(8, x), ko_oracle.kg_eval(9, x))
