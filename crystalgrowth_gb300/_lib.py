@@ -69,6 +69,7 @@ _SIGS = {
     "kg_device_fields": [_vp, ctypes.POINTER(_dp), ctypes.POINTER(_dp), ctypes.POINTER(_dp)],
     "kg_get_stream": [_vp, ctypes.POINTER(_vp)],
     "kg_set_graph_chunk": [_vp, ctypes.c_int],
+    "kg_step_noalloc": [ctypes.c_int, ctypes.c_int, ctypes.POINTER(Params), _vp, _vp, _vp, ctypes.c_longlong, _vp],
     "kg_last_error": [],
     "kg_version": [],
     "kg_diag_eval": [ctypes.c_int, _dp, _dp, ctypes.c_longlong, ctypes.c_double],

@@ -112,6 +112,26 @@ KG_API int kg_get_counters(const kg_sim* h, long long* steps, long long* frames)
 KG_API int kg_device_fields(kg_sim* h, double** phi, double** T, double** theta);
 KG_API int kg_get_stream(kg_sim* h, void** stream);
 
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they step the model -- a viewer or game loop that owns the GPU
+ * memory budget and allows no allocation inside a frame, a host recording its
+ * work while a CUDA stream is being captured (cudaMalloc/cudaFree are illegal
+ * then), a real-time loop that cannot afford cudaFree's device-wide
+ * synchronisation: advances the caller's own device buffers phi, T, theta
+ * (nx*ny FP64 each) in place by nsteps steps, enqueued on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream), and allocates nothing.
+ * The second copy of the state lives in a fixed device array inside the
+ * library (6 MiB per GPU that loads the library, held until exit), so grids
+ * are limited to 262,144 cells (512 x 512); larger ones are refused with
+ * KG_ERR_INVALID.  The first call on each device looks up that array's device
+ * address and keeps it: make that first call before any stream capture.  All
+ * calls on a device share the array, so calls that overlap on the GPU (e.g. on
+ * two streams at once) race and corrupt each other; nothing in the array needs
+ * to start at zero, each call overwrites what it reads.  Returns once the work
+ * is enqueued; synchronise the stream before reading the buffers. */
+KG_API int kg_step_noalloc(int nx, int ny, const kg_params* p, double* phi, double* T, double* theta,
+                           long long nsteps, void* stream);
+
 /* Steps per captured CUDA graph used by kg_step (default 100; 0 = no graphs). */
 KG_API int kg_set_graph_chunk(kg_sim* h, int chunk);
 
