@@ -53,6 +53,8 @@ _lib = None
 _SIGS = {
     "kg_params_default": [ctypes.POINTER(Params), ctypes.c_double],
     "kg_params_validate": [ctypes.POINTER(Params)],
+    "kg_slider_range": [ctypes.c_int, _ip, _ip, _ip],
+    "kg_params_from_sliders": [_ip, ctypes.c_double, ctypes.POINTER(Params)],
     "kg_create": [ctypes.c_int, ctypes.c_int, ctypes.POINTER(Params), ctypes.POINTER(_vp)],
     "kg_destroy": [_vp],
     "kg_reset": [_vp],
@@ -69,6 +71,12 @@ _SIGS = {
     "kg_device_fields": [_vp, ctypes.POINTER(_dp), ctypes.POINTER(_dp), ctypes.POINTER(_dp)],
     "kg_get_stream": [_vp, ctypes.POINTER(_vp)],
     "kg_set_graph_chunk": [_vp, ctypes.c_int],
+    "kg_set_tile": [_vp, ctypes.c_int, ctypes.c_int],
+    "kg_colormap": [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)],
+    "kg_save": [_vp, ctypes.c_char_p],
+    "kg_load": [_vp, ctypes.c_char_p],
+    "kg_colormap_device": [_vp, ctypes.c_int, _vp],
+    "kg_get_tile": [_vp, _ip, _ip],
     "kg_step_noalloc": [ctypes.c_int, ctypes.c_int, ctypes.POINTER(Params), _vp, _vp, _vp, ctypes.c_longlong, _vp],
     "kg_last_error": [],
     "kg_version": [],

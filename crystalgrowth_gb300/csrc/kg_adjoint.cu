@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(KG_ADJ_THREADS) kg_adj_seed(long long N, const
 struct kg_adjoint {
     int nx = 0, ny = 0;
     long long N = 0, nsteps = 0;
-    int k = 64, ncp = 0, bh = 64;
+    int k = 64, ncp = 0, nt = 128, bh = 64;
     kg_params p{};
     KgDev dev{};
     KgAdj adj{};
@@ -293,7 +293,7 @@ extern "C" int kg_adjoint_create(int nx, int ny, const kg_params* p, long long n
     a->nsteps = nsteps;
     a->k = (int)(checkpoint_every < nsteps ? checkpoint_every : nsteps);
     a->ncp = (int)((nsteps + a->k - 1) / a->k);
-    a->bh = ny < 64 ? ny : 64;
+    kg_pick_tile(nx, ny, &a->nt, &a->bh);
     const size_t N = (size_t)a->N, d = sizeof(double);
     cudaError_t e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess)
@@ -390,7 +390,10 @@ __global__ void __launch_bounds__(NT) kg_adj_fwd_kernel(const __grid_constant__ 
                  sm);
 }
 
-static dim3 adj_grid(const kg_adjoint* a) { return dim3((a->nx + 125) / 126, (a->ny + a->bh - 1) / a->bh); }
+static dim3 adj_grid(const kg_adjoint* a)
+{
+    return dim3((a->nx + a->nt - 3) / (a->nt - 2), (a->ny + a->bh - 1) / a->bh);
+}
 
 static double* st_ptr(kg_adjoint* a, int c) { return a->st + (size_t)c * 3 * a->N; }
 
@@ -406,8 +409,15 @@ static int adj_forward(kg_adjoint* a, int* cur_out)
                                     cudaMemcpyDeviceToDevice, a->stream));
         double* s = st_ptr(a, cur);
         double* d = st_ptr(a, cur ^ 1);
-        kg_adj_fwd_kernel<128><<<adj_grid(a), 128, 0, a->stream>>>(a->dev, a->nx, a->ny, a->bh, s, s + N, s + 2 * N, d,
-                                                                    d + N, d + 2 * N);
+        if (a->nt == 32)
+            kg_adj_fwd_kernel<32><<<adj_grid(a), 32, 0, a->stream>>>(a->dev, a->nx, a->ny, a->bh, s, s + N, s + 2 * N,
+                                                                      d, d + N, d + 2 * N);
+        else if (a->nt == 64)
+            kg_adj_fwd_kernel<64><<<adj_grid(a), 64, 0, a->stream>>>(a->dev, a->nx, a->ny, a->bh, s, s + N, s + 2 * N,
+                                                                      d, d + N, d + 2 * N);
+        else
+            kg_adj_fwd_kernel<128><<<adj_grid(a), 128, 0, a->stream>>>(a->dev, a->nx, a->ny, a->bh, s, s + N,
+                                                                        s + 2 * N, d, d + N, d + 2 * N);
         cur ^= 1;
     }
     KG_CUDA(cudaGetLastError());
@@ -500,9 +510,18 @@ extern "C" int kg_adjoint_gradient(kg_adjoint* a, kg_grad_result* out, double* d
         for (long long n = n0; n < n1; n++) {
             double* s = st_ptr(a, c);
             double* d = st_ptr(a, c ^ 1);
-            kg_tape_step_kernel<128><<<adj_grid(a), 128, 0, a->stream>>>(a->dev, a->nx, a->ny, a->bh, s, s + N,
-                                                                          s + 2 * N, d, d + N, d + 2 * N,
-                                                                          tape_slot(a, (int)(n - n0)));
+            if (a->nt == 32)
+                kg_tape_step_kernel<32><<<adj_grid(a), 32, 0, a->stream>>>(a->dev, a->nx, a->ny, a->bh, s, s + N,
+                                                                            s + 2 * N, d, d + N, d + 2 * N,
+                                                                            tape_slot(a, (int)(n - n0)));
+            else if (a->nt == 64)
+                kg_tape_step_kernel<64><<<adj_grid(a), 64, 0, a->stream>>>(a->dev, a->nx, a->ny, a->bh, s, s + N,
+                                                                            s + 2 * N, d, d + N, d + 2 * N,
+                                                                            tape_slot(a, (int)(n - n0)));
+            else
+                kg_tape_step_kernel<128><<<adj_grid(a), 128, 0, a->stream>>>(a->dev, a->nx, a->ny, a->bh, s, s + N,
+                                                                              s + 2 * N, d, d + N, d + 2 * N,
+                                                                              tape_slot(a, (int)(n - n0)));
             c ^= 1;
         }
         KG_CUDA(cudaGetLastError());

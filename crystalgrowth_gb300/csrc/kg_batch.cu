@@ -159,8 +159,8 @@ static int batch_check(const kg_batch* b)
 
 static int valid_tuning(const kg_batch_tuning* t)
 {
-    if (!(t->nt == 64 || t->nt == 128 || t->nt == 256))
-        return kg_fail(KG_ERR_INVALID, "batch tuning: nt must be 64, 128 or 256");
+    if (!(t->nt == 32 || t->nt == 64 || t->nt == 128 || t->nt == 256))
+        return kg_fail(KG_ERR_INVALID, "batch tuning: nt must be 32, 64, 128 or 256");
     if (t->bh < 4 || t->bh > 4096)
         return kg_fail(KG_ERR_INVALID, "batch tuning: bh must lie in [4, 4096]");
     if (t->mode != KG_BATCH_LAUNCH && t->mode != KG_BATCH_PERSISTENT)
@@ -208,6 +208,7 @@ static int batch_launch_step(kg_batch* b, int from)
 {
     cudaError_t e;
     switch (b->tune.nt) {
+    case 32: e = launch_one<32>(b, from); break;
     case 64: e = launch_one<64>(b, from); break;
     case 256: e = launch_one<256>(b, from); break;
     default: e = launch_one<128>(b, from); break;
@@ -241,6 +242,7 @@ static int persistent_run(kg_batch* b, int from, int nsteps)
 static int batch_persistent(kg_batch* b, int from, int nsteps)
 {
     switch (b->tune.nt) {
+    case 32: return persistent_run<32>(b, from, nsteps);
     case 64: return persistent_run<64>(b, from, nsteps);
     case 256: return persistent_run<256>(b, from, nsteps);
     default: return persistent_run<128>(b, from, nsteps);
@@ -571,8 +573,8 @@ extern "C" int kg_batch_autotune(kg_batch* b, int trial_steps, kg_batch_tuning* 
         cudaFree(saved);
         return kg_cuda_fail(e, "kg_batch_autotune setup");
     }
-    const int nts[3] = {64, 128, 256};
-    const int bhs[4] = {16, 32, 64, 128};
+    const int nts[3] = {32, 64, 128};
+    const int bhs[4] = {8, 16, 32, 64};
     const int modes[2] = {KG_BATCH_LAUNCH, KG_BATCH_PERSISTENT};
     for (int mi = 0; mi < 2 && rc == KG_OK; mi++)
         for (int ni = 0; ni < 3 && rc == KG_OK; ni++)

@@ -48,6 +48,64 @@ extern "C" int kg_params_default(kg_params* p, double dt)
     return KG_OK;
 }
 
+/* The reference's slider model (src/Kobayashi.cpp:12-59): per parameter the
+ * integer slider range, its default position (_parameterInit, :87-95) and the
+ * ratio that turns a position into a value (value = (float)position * ratio,
+ * the SB_THUMBTRACK branch of iWMHScroll, :587-591). */
+static const struct {
+    int lo, hi, def;
+    float ratio;
+} kg_sliders[KG_SLIDERS] = {
+    {1, 9, 3, 0.0001f},  /* tau */
+    {6, 15, 10, 0.001f}, /* eps_bar */
+    {5, 14, 10, 0.1f},   /* mu */
+    {10, 19, 16, 0.1f},  /* K */
+    {1, 9, 5, 0.01f},    /* delta */
+    {2, 8, 6, 1.0f},     /* aniso */
+    {7, 12, 9, 0.1f},    /* alpha */
+    {10, 20, 10, 1.0f},  /* gamma */
+    {5, 15, 10, 0.1f},   /* teq */
+};
+
+extern "C" int kg_slider_range(int which, int* lo, int* hi, int* def)
+{
+    if (which < 0 || which >= KG_SLIDERS)
+        return kg_fail(KG_ERR_INVALID, "kg_slider_range: slider %d out of range [0, %d)", which, KG_SLIDERS);
+    if (lo)
+        *lo = kg_sliders[which].lo;
+    if (hi)
+        *hi = kg_sliders[which].hi;
+    if (def)
+        *def = kg_sliders[which].def;
+    return KG_OK;
+}
+
+extern "C" int kg_params_from_sliders(const int* pos, double dt, kg_params* p)
+{
+    if (!pos || !p)
+        return kg_fail(KG_ERR_INVALID, "kg_params_from_sliders: null pointer");
+    float v[KG_SLIDERS];
+    for (int k = 0; k < KG_SLIDERS; k++) {
+        if (pos[k] < kg_sliders[k].lo || pos[k] > kg_sliders[k].hi)
+            return kg_fail(KG_ERR_INVALID, "kg_params_from_sliders: slider %d at %d outside [%d, %d]", k, pos[k],
+                           kg_sliders[k].lo, kg_sliders[k].hi);
+        v[k] = (float)pos[k] * kg_sliders[k].ratio;
+    }
+    int rc = kg_params_default(p, dt);
+    if (rc)
+        return rc;
+    p->tau = v[0];
+    p->eps_bar = v[1];
+    p->mu = v[2];
+    p->K = v[3];
+    p->delta = v[4];
+    p->aniso = v[5];
+    p->alpha = v[6];
+    p->gamma = v[7];
+    p->teq = v[8];
+    return kg_params_validate(p);
+}
+
 static bool finite_all(const kg_params* p)
 {
     const double* v = &p->dx;
@@ -117,6 +175,25 @@ int kg_prepare(const kg_params* p, KgDev* d)
     d->u0 = p->gamma * (p->teq - 0.0);
     d->m0 = d->a_pi * kg_atan(d->u0);
     return KG_OK;
+}
+
+/* Strip shape for one grid: the largest strips that still give the GPU about
+ * 30,000 CTAs (measured on GB300: below that, strips covering the growing
+ * crystals finish last and the SMs idle; above it, the repeated halo rows of
+ * short strips cost more than they save), down to one-warp strips of 4 rows. */
+void kg_pick_tile(int nx, int ny, int* nt, int* bh)
+{
+    const long long want = 30000;
+    const int shapes[8][2] = {{128, 64}, {128, 32}, {128, 16}, {64, 16}, {64, 8}, {32, 8}, {32, 4}};
+    for (int k = 0; k < 7; k++) {
+        int t = shapes[k][0], h = shapes[k][1];
+        long long ctas = (long long)((nx + t - 3) / (t - 2)) * ((ny + h - 1) / h);
+        if (ctas >= want || k == 6) {
+            *nt = t;
+            *bh = h < ny ? h : ny;
+            return;
+        }
+    }
 }
 
 __global__ void kg_seed_kernel(double* phi, double* t, double* theta, int nx, int ny, int n, const int* cx,

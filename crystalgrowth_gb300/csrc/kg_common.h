@@ -26,6 +26,12 @@ int kg_cuda_fail(cudaError_t e, const char* what);
 /* fills the derived constants of one parameter set; returns KG_OK or KG_ERR_INVALID */
 int kg_prepare(const kg_params* p, KgDev* d);
 
-/* zero fields and seed disks on the device (kg_seed.cu) */
+/* strip width (threads) and height for a single nx x ny grid on the current device */
+void kg_pick_tile(int nx, int ny, int* nt, int* bh);
+
+/* phi -> RGBA float32 for nx*ny cells in the given order (kg_color.cu) */
+int kg_color_launch(const double* phi, float* rgba, int nx, int ny, int order, cudaStream_t s);
+
+/* zero fields and seed disks on the device (kg_common.cu) */
 int kg_seed_device(double* phi, double* t, double* theta, int nx, int ny, int n, const int* cx, const int* cy,
                    const int* r, cudaStream_t s);

@@ -240,7 +240,11 @@ __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const d
         const size_t roff = (size_t)kg_wrap(r, ny) * nx;
         sm.t[r & 3][L] = t_in[roff + col];
         double theta = th_in[roff + col];
-        __syncthreads();
+        /* a one-warp strip (NT = 32) needs no CTA barrier: warps never wait on each other */
+        if constexpr (NT == 32)
+            __syncwarp();
+        else
+            __syncthreads();
 
         /* stage 1 at row r for all NT lanes */
         KgS1 s1 = kg_stage1(P, sm.phi[r & 7][L + 2], sm.phi[r & 7][L], sm.phi[(r + 1) & 7][L + 1],

@@ -6,16 +6,13 @@
  * (src/Kobayashi.h:107-115).  kg_step launches one fused kernel per time step
  * (kg_device.cuh) and replays them as CUDA graphs of `chunk` steps.
  */
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 #include <new>
 #include "kg_common.h"
+#include "kobayashi_color.h"
 
-#ifndef KG_NT
-#define KG_NT 128 /* threads (= columns incl. 2 halo) per strip */
-#endif
-#ifndef KG_BH
-#define KG_BH 64  /* rows per strip */
-#endif
 
 template <int NT>
 __global__ void __launch_bounds__(NT) kg_step_kernel(const __grid_constant__ KgDev P, int nx, int ny, int bh,
@@ -38,7 +35,9 @@ struct kg_sim {
     long long steps = 0, frames = 0;
     int chunk = 100;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    int bh = KG_BH;
+    int nt = 128; /* threads per strip CTA (strip width nt - 2 columns) */
+    int bh = 64;  /* rows per strip */
+    float* color = nullptr; /* RGBA staging buffer for kg_colormap, allocated on first use */
 };
 
 static void drop_graphs(kg_sim* h)
@@ -52,11 +51,16 @@ static void drop_graphs(kg_sim* h)
 
 static int launch_step(kg_sim* h, int from)
 {
-    const int NT = KG_NT;
-    dim3 grid((h->nx + NT - 3) / (NT - 2), (h->ny + h->bh - 1) / h->bh);
+    dim3 grid((h->nx + h->nt - 3) / (h->nt - 2), (h->ny + h->bh - 1) / h->bh);
     double* const* a = h->buf[from];
     double* const* b = h->buf[from ^ 1];
-    kg_step_kernel<NT><<<grid, NT, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1], b[2]);
+    if (h->nt == 32)
+        kg_step_kernel<32><<<grid, 32, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1], b[2]);
+    else if (h->nt == 64)
+        kg_step_kernel<64><<<grid, 64, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1], b[2]);
+    else
+        kg_step_kernel<128><<<grid, 128, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1],
+                                                          b[2]);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return kg_cuda_fail(e, "kg_step_kernel launch");
@@ -109,6 +113,8 @@ extern "C" int kg_destroy(kg_sim* h)
         for (int f = 0; f < 3; f++)
             if (h->buf[k][f])
                 cudaFree(h->buf[k][f]);
+    if (h->color)
+        cudaFree(h->color);
     if (h->stream)
         cudaStreamDestroy(h->stream);
     delete h;
@@ -157,8 +163,7 @@ extern "C" int kg_create(int nx, int ny, const kg_params* p, kg_sim** out)
     h->ny = ny;
     h->p = *p;
     h->dev = dev;
-    if (ny < h->bh)
-        h->bh = ny;
+    kg_pick_tile(nx, ny, &h->nt, &h->bh);
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     size_t bytes = sizeof(double) * (size_t)nx * ny;
     for (int k = 0; k < 2 && e == cudaSuccess; k++)
@@ -213,6 +218,34 @@ extern "C" int kg_set_graph_chunk(kg_sim* h, int chunk)
         return kg_fail(KG_ERR_INVALID, "kg_set_graph_chunk: chunk %d out of range", chunk);
     h->chunk = chunk;
     drop_graphs(h);
+    return KG_OK;
+}
+
+extern "C" int kg_set_tile(kg_sim* h, int nt, int bh)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (nt != 32 && nt != 64 && nt != 128)
+        return kg_fail(KG_ERR_INVALID, "kg_set_tile: nt must be 32, 64 or 128");
+    if (bh < 1 || bh > 65536)
+        return kg_fail(KG_ERR_INVALID, "kg_set_tile: bh must lie in [1, 65536]");
+    KG_CUDA(cudaStreamSynchronize(h->stream));
+    h->nt = nt;
+    h->bh = bh < h->ny ? bh : h->ny;
+    drop_graphs(h);
+    return KG_OK;
+}
+
+extern "C" int kg_get_tile(const kg_sim* h, int* nt, int* bh)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (nt)
+        *nt = h->nt;
+    if (bh)
+        *bh = h->bh;
     return KG_OK;
 }
 
@@ -338,5 +371,175 @@ extern "C" int kg_get_stream(kg_sim* h, void** stream)
     if (!stream)
         return kg_fail(KG_ERR_INVALID, "kg_get_stream: null pointer");
     *stream = (void*)h->stream;
+    return KG_OK;
+}
+
+extern "C" int kg_colormap_device(kg_sim* h, int order, float* rgba_device)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (!rgba_device)
+        return kg_fail(KG_ERR_INVALID, "kg_colormap_device: null buffer");
+    return kg_color_launch(h->buf[h->cur][0], rgba_device, h->nx, h->ny, order, h->stream);
+}
+
+extern "C" int kg_colormap(kg_sim* h, int order, float* rgba)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (!rgba)
+        return kg_fail(KG_ERR_INVALID, "kg_colormap: null buffer");
+    size_t bytes = sizeof(float) * 4 * (size_t)h->nx * h->ny;
+    if (!h->color)
+        KG_CUDA(cudaMalloc(&h->color, bytes));
+    rc = kg_color_launch(h->buf[h->cur][0], h->color, h->nx, h->ny, order, h->stream);
+    if (rc)
+        return rc;
+    KG_CUDA(cudaMemcpyAsync(rgba, h->color, bytes, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(cudaStreamSynchronize(h->stream));
+    return KG_OK;
+}
+
+/* ---- snapshots: a 4096-byte JSON header, then phi, T, theta as little-endian FP64 ---- */
+
+#define KG_SNAP_HEADER 4096
+
+static const char* kg_param_names[13] = {"dx", "dy", "dt", "tau", "eps_bar", "mu", "K",
+                                          "delta", "aniso", "alpha", "gamma", "teq", "theta0"};
+
+extern "C" int kg_save(kg_sim* h, const char* path)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (!path)
+        return kg_fail(KG_ERR_INVALID, "kg_save: null path");
+    char hdr[KG_SNAP_HEADER];
+    memset(hdr, ' ', sizeof hdr);
+    int n = snprintf(hdr, sizeof hdr,
+                     "{\"format\": \"kobayashi-gb300-snapshot\", \"version\": 1, \"nx\": %d, \"ny\": %d, "
+                     "\"steps\": %lld, \"frames\": %lld, \"dtype\": \"float64\", \"byteorder\": \"little\", "
+                     "\"fields\": [\"phi\", \"T\", \"theta\"], \"header_bytes\": %d, \"params\": {",
+                     h->nx, h->ny, h->steps, h->frames, KG_SNAP_HEADER);
+    const double* pv = &h->p.dx;
+    for (int k = 0; k < 13; k++)
+        n += snprintf(hdr + n, sizeof hdr - n, "%s\"%s\": %.17g", k ? ", " : "", kg_param_names[k], pv[k]);
+    n += snprintf(hdr + n, sizeof hdr - n, "}}");
+    if (n >= KG_SNAP_HEADER - 1)
+        return kg_fail(KG_ERR_INVALID, "kg_save: header overflow");
+    hdr[n] = ' ';
+    hdr[KG_SNAP_HEADER - 1] = '\n';
+    FILE* f = fopen(path, "wb");
+    if (!f)
+        return kg_fail(KG_ERR_INVALID, "kg_save: cannot open %s for writing", path);
+    size_t cells = (size_t)h->nx * h->ny;
+    double* buf = (double*)malloc(cells * sizeof(double));
+    rc = KG_OK;
+    if (!buf)
+        rc = kg_fail(KG_ERR_NOMEM, "kg_save: host buffer");
+    if (rc == KG_OK && fwrite(hdr, 1, sizeof hdr, f) != sizeof hdr)
+        rc = kg_fail(KG_ERR_INVALID, "kg_save: write failed");
+    for (int fld = 0; fld < 3 && rc == KG_OK; fld++) {
+        cudaError_t e = cudaMemcpyAsync(buf, h->buf[h->cur][fld], cells * sizeof(double), cudaMemcpyDeviceToHost,
+                                        h->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess)
+            rc = kg_cuda_fail(e, "kg_save: device copy");
+        else if (fwrite(buf, sizeof(double), cells, f) != cells)
+            rc = kg_fail(KG_ERR_INVALID, "kg_save: write failed");
+    }
+    free(buf);
+    if (fclose(f) != 0 && rc == KG_OK)
+        rc = kg_fail(KG_ERR_INVALID, "kg_save: close failed");
+    return rc;
+}
+
+static int snap_int(const char* hdr, const char* key, long long* v)
+{
+    char pat[64];
+    snprintf(pat, sizeof pat, "\"%s\": ", key);
+    const char* p = strstr(hdr, pat);
+    if (!p)
+        return -1;
+    return sscanf(p + strlen(pat), "%lld", v) == 1 ? 0 : -1;
+}
+
+static int snap_double(const char* hdr, const char* key, double* v)
+{
+    char pat[64];
+    snprintf(pat, sizeof pat, "\"%s\": ", key);
+    const char* p = strstr(hdr, pat);
+    if (!p)
+        return -1;
+    return sscanf(p + strlen(pat), "%lf", v) == 1 ? 0 : -1;
+}
+
+extern "C" int kg_load(kg_sim* h, const char* path)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (!path)
+        return kg_fail(KG_ERR_INVALID, "kg_load: null path");
+    FILE* f = fopen(path, "rb");
+    if (!f)
+        return kg_fail(KG_ERR_INVALID, "kg_load: cannot open %s", path);
+    char hdr[KG_SNAP_HEADER + 1];
+    size_t got = fread(hdr, 1, KG_SNAP_HEADER, f);
+    hdr[got] = 0;
+    long long nx = 0, ny = 0, steps = 0, frames = 0, version = 0;
+    if (got != KG_SNAP_HEADER || !strstr(hdr, "\"format\": \"kobayashi-gb300-snapshot\"") ||
+        snap_int(hdr, "version", &version) || version != 1 || snap_int(hdr, "nx", &nx) || snap_int(hdr, "ny", &ny) ||
+        snap_int(hdr, "steps", &steps) || snap_int(hdr, "frames", &frames)) {
+        fclose(f);
+        return kg_fail(KG_ERR_INVALID, "kg_load: %s is not a kobayashi-gb300 snapshot", path);
+    }
+    if (nx != h->nx || ny != h->ny) {
+        fclose(f);
+        return kg_fail(KG_ERR_INVALID, "kg_load: snapshot is %lld x %lld, the handle is %d x %d", nx, ny, h->nx, h->ny);
+    }
+    kg_params p;
+    double* pv = &p.dx;
+    for (int k = 0; k < 13; k++)
+        if (snap_double(hdr, kg_param_names[k], &pv[k])) {
+            fclose(f);
+            return kg_fail(KG_ERR_INVALID, "kg_load: parameter %s missing", kg_param_names[k]);
+        }
+    KgDev dev;
+    rc = kg_prepare(&p, &dev);
+    if (rc) {
+        fclose(f);
+        return rc;
+    }
+    size_t cells = (size_t)nx * ny;
+    double* buf = (double*)malloc(cells * sizeof(double));
+    if (!buf) {
+        fclose(f);
+        return kg_fail(KG_ERR_NOMEM, "kg_load: host buffer");
+    }
+    for (int fld = 0; fld < 3 && rc == KG_OK; fld++) {
+        if (fread(buf, sizeof(double), cells, f) != cells) {
+            rc = kg_fail(KG_ERR_INVALID, "kg_load: %s is truncated", path);
+            break;
+        }
+        cudaError_t e = cudaMemcpyAsync(h->buf[h->cur][fld], buf, cells * sizeof(double), cudaMemcpyHostToDevice,
+                                        h->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess)
+            rc = kg_cuda_fail(e, "kg_load: device copy");
+    }
+    free(buf);
+    fclose(f);
+    if (rc)
+        return rc;
+    h->p = p;
+    h->dev = dev;
+    h->steps = steps;
+    h->frames = frames;
+    drop_graphs(h);
     return KG_OK;
 }

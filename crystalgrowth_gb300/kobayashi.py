@@ -89,6 +89,28 @@ class Kobayashi:
     def set_graph_chunk(self, chunk):
         check(lib().kg_set_graph_chunk(self._h, int(chunk)))
 
+    def colormap(self, viewer_order=False):
+        """RGBA float32 of every cell (the reference's colour ramp, src/Kobayashi.cpp:309-345);
+        viewer_order=True reproduces the viewer's constant-buffer order and its transposition."""
+        out = np.empty((self.nx * self.ny, 4), dtype=np.float32)
+        check(lib().kg_colormap(self._h, 1 if viewer_order else 0, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out
+
+    def save(self, path):
+        """snapshot: JSON header + phi, T, theta (FP64)"""
+        check(lib().kg_save(self._h, str(path).encode()))
+
+    def load(self, path):
+        check(lib().kg_load(self._h, str(path).encode()))
+
+    def set_tile(self, nt, bh):
+        check(lib().kg_set_tile(self._h, int(nt), int(bh)))
+
+    def tile(self):
+        nt, bh = ctypes.c_int(), ctypes.c_int()
+        check(lib().kg_get_tile(self._h, ctypes.byref(nt), ctypes.byref(bh)))
+        return nt.value, bh.value
+
     def stream(self):
         s = ctypes.c_void_p()
         check(lib().kg_get_stream(self._h, ctypes.byref(s)))

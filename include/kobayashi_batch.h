@@ -20,7 +20,7 @@ extern "C" {
 #define KG_BATCH_PERSISTENT 1  /* one cooperative kernel per chunk, bounded grid barrier between steps */
 
 typedef struct kg_batch_tuning {
-    int nt;     /* threads per strip CTA: 64, 128 or 256 (strip width nt - 2 columns) */
+    int nt;     /* threads per strip CTA: 32, 64, 128 or 256 (strip width nt - 2 columns) */
     int bh;     /* rows per strip */
     int mode;   /* KG_BATCH_LAUNCH or KG_BATCH_PERSISTENT */
     int chunk;  /* steps per graph (launch mode) or per persistent launch */

@@ -62,6 +62,15 @@ KG_API int kg_params_default(kg_params* p, double dt);
  * value in [1, 64]. */
 KG_API int kg_params_validate(const kg_params* p);
 
+/* The reference's parameter sliders (src/Kobayashi.cpp:12-59, 555-618): nine
+ * integer positions in the order tau, eps_bar, mu, K, delta, aniso, alpha,
+ * gamma, teq; value = (float)position * ratio as the slider's thumb-track
+ * handler computes it (ratios 1e-4, 1e-3, 0.1, 0.1, 0.01, 1, 0.1, 1, 0.1).
+ * kg_slider_range gives a slider's integer range and default position. */
+#define KG_SLIDERS 9
+KG_API int kg_slider_range(int which, int* lo, int* hi, int* def);
+KG_API int kg_params_from_sliders(const int* pos, double dt, kg_params* p);
+
 /* Kobayashi(int x, int y, float timeStep) + _vectorInit (src/Kobayashi.cpp:7-67,
  * 98-123): allocates the grid on the current device, zeroes phi, T and theta
  * and seeds the reference's 5-cell nucleus at (nx/2, ny/2).  nx, ny >= 1
@@ -132,8 +141,22 @@ KG_API int kg_get_stream(kg_sim* h, void** stream);
 KG_API int kg_step_noalloc(int nx, int ny, const kg_params* p, double* phi, double* T, double* theta,
                            long long nsteps, void* stream);
 
+/* Strip shape of the fused step: nt threads per CTA (32, 64 or 128; the strip
+ * is nt - 2 columns wide) and bh rows per strip.  kg_create picks the largest
+ * strips that still give the GPU about 30,000 CTAs; results do not depend on
+ * the shape. */
+KG_API int kg_set_tile(kg_sim* h, int nt, int bh);
+KG_API int kg_get_tile(const kg_sim* h, int* nt, int* bh);
+
 /* Steps per captured CUDA graph used by kg_step (default 100; 0 = no graphs). */
 KG_API int kg_set_graph_chunk(kg_sim* h, int chunk);
+
+/* Snapshots (no counterpart in the reference, which keeps its state in memory
+ * only): a 4096-byte JSON header (format, version, nx, ny, steps, frames,
+ * params) followed by phi, T, theta as little-endian FP64 arrays.  kg_load
+ * needs a handle of the same size and restores parameters and counters. */
+KG_API int kg_save(kg_sim* h, const char* path);
+KG_API int kg_load(kg_sim* h, const char* path);
 
 /* Message of the calling thread's last failure ("" if none). */
 KG_API const char* kg_last_error(void);

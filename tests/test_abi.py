@@ -83,3 +83,31 @@ def test_null_handle_is_an_error_not_a_crash():
     assert lib.kg_destroy(None) == 0
     assert b"null" in lib.kg_last_error()
     assert lib.kg_version().startswith(b"kobayashi-gb300")
+
+
+def test_slider_model():
+    """the reference's integer sliders (src/Kobayashi.cpp:12-59): ranges, default positions, and
+    value = (float)position * ratio (iWMHScroll's thumb-track branch, :587-591)"""
+    import numpy as np
+    lib = kg.load()
+    rng = []
+    for k in range(9):
+        lo, hi, de = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        assert lib.kg_slider_range(k, ctypes.byref(lo), ctypes.byref(hi), ctypes.byref(de)) == 0
+        rng.append((lo.value, hi.value, de.value))
+    assert rng == [(1, 9, 3), (6, 15, 10), (5, 14, 10), (10, 19, 16), (1, 9, 5), (2, 8, 6), (7, 12, 9), (10, 20, 10),
+                   (5, 15, 10)]
+    assert lib.kg_slider_range(9, None, None, None) == _lib.KG_ERR_INVALID
+    pos = (ctypes.c_int * 9)(*[r[2] for r in rng])
+    p = kg.Params()
+    assert lib.kg_params_from_sliders(pos, 1e-4, ctypes.byref(p)) == 0
+    ratios = np.array([1e-4, 1e-3, 0.1, 0.1, 0.01, 1.0, 0.1, 1.0, 0.1], dtype=np.float32)
+    want = (np.array([r[2] for r in rng], dtype=np.float32) * ratios).astype(np.float64)
+    got = [p.tau, p.eps_bar, p.mu, p.K, p.delta, p.aniso, p.alpha, p.gamma, p.teq]
+    assert got == list(want)
+    # the slider defaults reproduce the reference's defaults to float precision
+    assert abs(p.tau - 0.0003) < 1e-10 and abs(p.K - 1.6) < 1e-6 and p.aniso == 6.0
+    bad = (ctypes.c_int * 9)(*[r[2] for r in rng])
+    bad[4] = 10
+    assert lib.kg_params_from_sliders(bad, 1e-4, ctypes.byref(p)) == _lib.KG_ERR_INVALID
+    assert b"outside" in lib.kg_last_error()

@@ -44,7 +44,7 @@ def oracle(inst, steps):
 
 
 @pytest.mark.parametrize("mode", [KG_BATCH_LAUNCH, KG_BATCH_PERSISTENT])
-@pytest.mark.parametrize("nt,bh,chunk", [(64, 16, 7), (128, 64, 100), (256, 32, 3)])
+@pytest.mark.parametrize("nt,bh,chunk", [(32, 8, 5), (64, 16, 7), (128, 64, 100), (256, 32, 3)])
 def test_batch_bitwise_vs_oracle(mode, nt, bh, chunk):
     inst = small_ensemble()
     steps = 41
@@ -79,7 +79,7 @@ def test_autotune_restores_state_and_keeps_results():
     b.step(5)
     before = [b.fields(k) for k in range(len(inst))]
     best, ms = b.autotune(trial_steps=3)
-    assert best["nt"] in (64, 128, 256) and ms > 0
+    assert best["nt"] in (32, 64, 128, 256) and ms > 0
     after = [b.fields(k) for k in range(len(inst))]
     for x, y in zip(before, after):
         for u, v in zip(x, y):
@@ -125,4 +125,22 @@ def test_batch_rejects_bad_input():
         b.set_tuning(nt=100)
     assert _lib.lib().kg_batch_get_fields(b._h, 3, None, None, None) == _lib.KG_ERR_INVALID
     assert b"out of range" in _lib.lib().kg_last_error()
+    b.close()
+
+
+def test_ensemble_512_full_length_sample():
+    """the 512-instance ensemble over its full 3000 steps; six instances (smallest, largest and
+    four others) checked against the CPU oracle bit for bit"""
+    cfg = configs.ensemble_512()
+    inst = cfg["instances"]
+    b = make_batch(inst)
+    best, _ = b.autotune(trial_steps=3)
+    b.step(cfg["steps"])
+    sides = [i["nx"] for i in inst]
+    picks = sorted({sides.index(min(sides)), sides.index(max(sides)), 7, 128, 300, 509})
+    for k in picks:
+        ref = ko_oracle.port_run(*configs.initial_fields(inst[k]["nx"], inst[k]["ny"], inst[k]["disks"]),
+                                 inst[k]["params"], cfg["steps"], threads=16)
+        for x, y in zip(b.fields(k), ref):
+            assert bits_equal(x, y), k
     b.close()

@@ -102,6 +102,22 @@ def test_graph_chunks_do_not_change_results():
             assert bits_equal(x, y)
 
 
+@pytest.mark.parametrize("nt,bh", [(32, 1), (32, 17), (64, 1), (64, 8), (128, 3), (128, 200)])
+def test_strip_shape_does_not_change_results(nt, bh):
+    p = dict(configs.BASE)
+    disks = [(70, 50, 6), (10, 90, 4)]
+    sim = Kobayashi(141, 103, p["dt"], params=p)
+    sim.seed_disks(disks)
+    sim.set_tile(nt, bh)
+    assert sim.tile() == (nt, min(bh, 103))
+    sim.step(90)
+    a = sim.fields()
+    sim.close()
+    b = oracle_run(141, 103, p, disks, 90)
+    for x, y in zip(a, b):
+        assert bits_equal(x, y)
+
+
 def test_translation_invariance_full_size():
     """periodic grid: shifting the nuclei shifts the solution exactly (every cell runs the same arithmetic)"""
     cfg = configs.grid_8192()
@@ -177,3 +193,27 @@ def test_invalid_arguments_fail_cleanly():
         sim.set_params(dx=float("nan"))
     sim.step(3)  # still usable
     sim.close()
+
+
+def test_variant_2048_full_length():
+    """one anisotropy variant of the 2048^2 set (j=4, delta=0.05, K=2.0, theta0=pi/4) over its full
+    5000 steps, against the CPU oracle, bit for bit"""
+    v = [x for x in configs.variants_2048() if x["params"]["aniso"] == 4.0 and x["params"]["delta"] == 0.05
+         and x["params"]["K"] == 2.0 and x["params"]["theta0"] > 0.7][0]
+    a = gpu_run(v["nx"], v["ny"], v["params"], v["disks"], v["steps"])
+    b = oracle_run(v["nx"], v["ny"], v["params"], v["disks"], v["steps"])
+    for x, y in zip(a, b):
+        assert bits_equal(x, y)
+
+
+def test_translation_invariance_grid8192_1000_steps():
+    """the 8192^2 workload over 1000 steps, nuclei shifted by (3001, 77): the solution shifts exactly"""
+    cfg = configs.grid_8192()
+    n = cfg["nx"]
+    di, dj = 3001, 77
+    shifted = [((x + di) % n, (y + dj) % n, r) for x, y, r in cfg["disks"]]
+    a = gpu_run(n, n, cfg["params"], cfg["disks"], 1000)
+    b = gpu_run(n, n, cfg["params"], shifted, 1000)
+    assert np.abs(a[0]).max() > 0.5  # crystals have grown
+    for x, y in zip(a, b):
+        assert bits_equal(np.roll(x, (dj, di), axis=(0, 1)), y)
