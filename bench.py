@@ -108,13 +108,23 @@ def measured_peak():
 
 
 def profile_traffic():
-    """DRAM bytes per launch of the step kernel from the committed ncu summary (null if absent)."""
+    """DRAM bytes and FP64 thread-operations per launch of the step kernel on the 8192^2 workload,
+    from the committed ncu summary (None if absent)."""
     try:
         with open(os.path.join(ROOT, "profiles", "kg_step_kernel_traffic.json")) as f:
             d = json.load(f)
         return d.get("bytes_per_launch_8192"), d
     except (OSError, ValueError):
-        return None, None
+        return None, {}
+
+
+def fp64_peak():
+    """FP64 FMA lane-operations per second of this GPU, measured now (kg_diag_fp64_peak)."""
+    import ctypes
+    from crystalgrowth_gb300 import _lib
+    v = ctypes.c_double()
+    _lib.check(_lib.lib().kg_diag_fp64_peak(ctypes.byref(v)))
+    return v.value
 
 
 def cpu_baseline_sample(cfg, seconds_budget=20.0):
@@ -354,7 +364,16 @@ def run_ours(args, rank, world):
 
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_CELL * cells / launch_s / 1e9
-    traffic, _ = profile_traffic()
+    traffic, prof = profile_traffic()
+    fp64 = None
+    ops = prof.get("fp64_thread_ops_per_launch_8192") if nx == 8192 and ny == 8192 else None
+    if ops:
+        pk = fp64_peak()
+        fp64 = {"bound": "fp64 pipe", "achieved": ops / launch_s / 1e9, "peak": pk / 1e9, "unit": "GFLOP-ops/s",
+                "frac": ops / launch_s / pk, "ops_per_cell_update": ops / cells,
+                "peak_kind": "measured now (kg_diag_fp64_peak, DFMA lanes/s)",
+                "ops_source": "ncu DADD+DMUL+DFMA thread instructions of one mid-window launch "
+                              "(profiles/kg_step_kernel_traffic.json)"}
     line = {"metric": "fp64_cell_updates_per_s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -367,6 +386,7 @@ def run_ours(args, rank, world):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "note": "48 B/cell algorithmic; the kernel is FP64-pipe bound on GB300"},
+            "fp64_roofline": fp64,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": 3 * 8 * cells,
                     "d2h_bytes_per_step": 3 * 8 * cells},
             "gpu_launches": args.steps * CHUNK,

@@ -11,7 +11,8 @@
  *   phi' = phi + R dt / tau,  T' = T + lap(T) dt + K (phi' - phi)
  *
  * Reverse of one step, given the adjoints (lphi', lT', ltheta') of the next
- * state, in three gather passes over the tape of the step:
+ * state, in gather passes over the tape of the step (A and B run as one
+ * kernel, kg_adj_pass_ab, which recomputes the neighbours' lR):
  *   A (local):  lR = (lphi' + K lT') dt/tau, the Laplacian seeds lR e2 and lT' dt,
  *               the local parts of lphi and lT, and the K, tau, gamma gradients;
  *   B (radius 1): the adjoints of e2, a, b gathered from the neighbours' lR,
@@ -70,50 +71,21 @@ __device__ void kg_block_accumulate(double v[KG_NPARAM], double* part)
 }
 
 struct KgAdjWork {
-    double *lR, *lLphi, *lLT, *lphi_loc, *lT_loc, *lgx, *lgy;
+    double *lLphi, *lLT, *lphi_loc, *lT_loc, *lgx, *lgy;
 };
-
-__global__ void __launch_bounds__(KG_ADJ_THREADS) kg_adj_pass_a(const __grid_constant__ KgAdj A, long long N,
-                                                                const __grid_constant__ KgTape tp,
-                                                                const double* __restrict__ phi_next,
-                                                                const double* __restrict__ lphi1,
-                                                                const double* __restrict__ lt1,
-                                                                const __grid_constant__ KgAdjWork w, double* part)
-{
-    double g[KG_NPARAM] = {0, 0, 0, 0, 0};
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N; c += (long long)gridDim.x * blockDim.x) {
-        double phi = tp.f[KG_TAPE_PHI][c], t = tp.f[KG_TAPE_T][c];
-        double lap = tp.f[KG_TAPE_LAP][c], R = tp.f[KG_TAPE_RHS][c], m = tp.f[KG_TAPE_M][c];
-        double eps = A.eb * (1.0 + A.delta * tp.f[KG_TAPE_COS][c]);
-        double lp = lphi1[c], lt = lt1[c];
-        double lam = lp + A.K * lt;
-        double lR = lam * A.dt_tau;
-        double q = phi - 0.5 + m;
-        double pp = phi * (1.0 - phi);
-        double dw = (1.0 - 2.0 * phi) * q + pp;
-        double lm = lR * pp;
-        double u = A.gamma * (A.teq - t);
-        double inv = (u == A.u0) ? A.inv0 : 1.0 / (1.0 + u * u);
-        w.lR[c] = lR;
-        w.lLphi[c] = lR * eps * eps;
-        w.lLT[c] = lt * A.dt;
-        w.lphi_loc[c] = lp + lR * dw;
-        w.lT_loc[c] = lt - lm * A.a_pi * A.gamma * inv;
-        g[1] += lt * (phi_next[c] - phi);        /* K */
-        g[3] += -lR * R / A.tau;                 /* tau */
-        g[4] += lm * A.a_pi * (A.teq - t) * inv; /* gamma */
-        (void)lap;
-    }
-    kg_block_accumulate(g, part);
-}
 
 __device__ __forceinline__ long long kg_nb(int i, int j, int nx) { return (long long)j * nx + i; }
 
-__global__ void __launch_bounds__(KG_ADJ_THREADS) kg_adj_pass_b(const __grid_constant__ KgAdj A, int nx, int ny,
-                                                                const __grid_constant__ KgTape tp,
-                                                                const double* __restrict__ lth1,
-                                                                double* __restrict__ lth0,
-                                                                const __grid_constant__ KgAdjWork w, double* part)
+/* Passes A and B in one sweep: the neighbours' lR = (lphi' + K lT') dt/tau is
+ * recomputed from the next step's adjoints instead of being read back. */
+__global__ void __launch_bounds__(KG_ADJ_THREADS) kg_adj_pass_ab(const __grid_constant__ KgAdj A, int nx, int ny,
+                                                                 const __grid_constant__ KgTape tp,
+                                                                 const double* __restrict__ phi_next,
+                                                                 const double* __restrict__ lphi1,
+                                                                 const double* __restrict__ lt1,
+                                                                 const double* __restrict__ lth1,
+                                                                 double* __restrict__ lth0,
+                                                                 const __grid_constant__ KgAdjWork w, double* part)
 {
     const long long N = (long long)nx * ny;
     double g[KG_NPARAM] = {0, 0, 0, 0, 0};
@@ -122,16 +94,35 @@ __global__ void __launch_bounds__(KG_ADJ_THREADS) kg_adj_pass_b(const __grid_con
         int ip = i + 1 == nx ? 0 : i + 1, im = i == 0 ? nx - 1 : i - 1;
         int jp = j + 1 == ny ? 0 : j + 1, jm = j == 0 ? ny - 1 : j - 1;
         long long cE = kg_nb(ip, j, nx), cW = kg_nb(im, j, nx), cN = kg_nb(i, jp, nx), cS = kg_nb(i, jm, nx);
-        const double* GX = tp.f[KG_TAPE_GX];
-        const double* GY = tp.f[KG_TAPE_GY];
-        double lRc = w.lR[c], lRE = w.lR[cE], lRW = w.lR[cW], lRN = w.lR[cN], lRS = w.lR[cS];
-        double gx = GX[c], gy = GY[c];
-        double le2 = lRc * tp.f[KG_TAPE_LAP][c] + (lRW * GX[cW] - lRE * GX[cE]) * A.inv_dx +
-                     (lRS * GY[cS] - lRN * GY[cN]) * A.inv_dy;
-        double la = (lRS - lRN) * A.inv_dy;
-        double lb = (lRE - lRW) * A.inv_dx;
+        /* pass A at c */
+        double phi = tp.f[KG_TAPE_PHI][c], t = tp.f[KG_TAPE_T][c];
+        double lap = tp.f[KG_TAPE_LAP][c], R = tp.f[KG_TAPE_RHS][c], m = tp.f[KG_TAPE_M][c];
         double s = tp.f[KG_TAPE_SIN][c], co = tp.f[KG_TAPE_COS][c];
         double eps = A.eb * (1.0 + A.delta * co);
+        double lp = lphi1[c], lt = lt1[c];
+        double lRc = (lp + A.K * lt) * A.dt_tau;
+        double q = phi - 0.5 + m;
+        double pp = phi * (1.0 - phi);
+        double dw = (1.0 - 2.0 * phi) * q + pp;
+        double lm = lRc * pp;
+        double u = A.gamma * (A.teq - t);
+        double inv = (u == A.u0) ? A.inv0 : 1.0 / (1.0 + u * u);
+        w.lLphi[c] = lRc * eps * eps;
+        w.lLT[c] = lt * A.dt;
+        w.lphi_loc[c] = lp + lRc * dw;
+        w.lT_loc[c] = lt - lm * A.a_pi * A.gamma * inv;
+        g[1] += lt * (phi_next[c] - phi);
+        g[3] += -lRc * R / A.tau;
+        g[4] += lm * A.a_pi * (A.teq - t) * inv;
+        /* pass B at c, with the neighbours' lR recomputed */
+        double lRE = (lphi1[cE] + A.K * lt1[cE]) * A.dt_tau, lRW = (lphi1[cW] + A.K * lt1[cW]) * A.dt_tau;
+        double lRN = (lphi1[cN] + A.K * lt1[cN]) * A.dt_tau, lRS = (lphi1[cS] + A.K * lt1[cS]) * A.dt_tau;
+        const double* GX = tp.f[KG_TAPE_GX];
+        const double* GY = tp.f[KG_TAPE_GY];
+        double gx = GX[c], gy = GY[c];
+        double le2 = lRc * lap + (lRW * GX[cW] - lRE * GX[cE]) * A.inv_dx + (lRS * GY[cS] - lRN * GY[cN]) * A.inv_dy;
+        double la = (lRS - lRN) * A.inv_dy;
+        double lb = (lRE - lRW) * A.inv_dx;
         double epsd = -A.eb * A.j * A.delta * s;
         double ee = eps * epsd;
         double lq = la * gx + lb * gy;
@@ -140,10 +131,9 @@ __global__ void __launch_bounds__(KG_ADJ_THREADS) kg_adj_pass_b(const __grid_con
         double lgx = lRc * tp.f[KG_TAPE_GEX][c] + la * ee;
         double lgy = lRc * tp.f[KG_TAPE_GEY][c] + lb * ee;
         double lpsi = leps * (-A.eb * A.delta * s) + lepsd * (-A.eb * A.j * A.delta * co);
-        g[0] += leps * A.eb * co + lepsd * (-A.eb * A.j * s); /* delta */
-        g[2] += -A.j * lpsi;                                  /* theta0 */
+        g[0] += leps * A.eb * co + lepsd * (-A.eb * A.j * s);
+        g[2] += -A.j * lpsi;
         double lthp = lth1[c] + A.j * lpsi;
-        /* the angle branch taken in the forward step (same tests as kg_stage1) */
         uint64_t bx = kg_bits(gx), by = kg_bits(gy);
         bool gx_small = kg_small(bx), gx_pos = kg_pos_big(bx), gx_neg = kg_neg_big(bx);
         bool gy_big = kg_pos_big(by) || kg_neg_big(by);
@@ -153,7 +143,7 @@ __global__ void __launch_bounds__(KG_ADJ_THREADS) kg_adj_pass_b(const __grid_con
             lgx += lthp * (-gy) * r2;
             lgy += lthp * gx * r2;
         } else if (!(gx_small && gy_big)) {
-            lth = lthp; /* dead zone: theta' = theta */
+            lth = lthp;
         }
         w.lgx[c] = lgx;
         w.lgy[c] = lgy;
@@ -224,7 +214,7 @@ struct kg_adjoint {
     double* st = nullptr;     /* 2 * 3N */
     double* tape = nullptr;   /* k * KG_TAPE_FIELDS * N */
     double* lam = nullptr;    /* 2 * 3N */
-    double* work = nullptr;   /* 7N */
+    double* work = nullptr;   /* 6N */
     double* part = nullptr;   /* KG_ADJ_BLOCKS * KG_NPARAM + KG_ADJ_BLOCKS */
 };
 
@@ -309,7 +299,7 @@ extern "C" int kg_adjoint_create(int nx, int ny, const kg_params* p, long long n
     if (e == cudaSuccess)
         e = cudaMalloc(&a->lam, 6 * N * d);
     if (e == cudaSuccess)
-        e = cudaMalloc(&a->work, 7 * N * d);
+        e = cudaMalloc(&a->work, 6 * N * d);
     if (e == cudaSuccess)
         e = cudaMalloc(&a->part, (KG_ADJ_BLOCKS * KG_NPARAM + KG_ADJ_BLOCKS) * d);
     if (e == cudaSuccess)
@@ -494,13 +484,12 @@ extern "C" int kg_adjoint_gradient(kg_adjoint* a, kg_grad_result* out, double* d
         return rc;
     KG_CUDA(cudaMemsetAsync(a->part, 0, sizeof(double) * KG_ADJ_BLOCKS * KG_NPARAM, a->stream));
     KgAdjWork w;
-    w.lR = a->work;
-    w.lLphi = a->work + N;
-    w.lLT = a->work + 2 * N;
-    w.lphi_loc = a->work + 3 * N;
-    w.lT_loc = a->work + 4 * N;
-    w.lgx = a->work + 5 * N;
-    w.lgy = a->work + 6 * N;
+    w.lLphi = a->work;
+    w.lLT = a->work + N;
+    w.lphi_loc = a->work + 2 * N;
+    w.lT_loc = a->work + 3 * N;
+    w.lgx = a->work + 4 * N;
+    w.lgy = a->work + 5 * N;
     int lc = 0; /* lam copy holding the adjoint of the state after the current step */
     for (int seg = a->ncp - 1; seg >= 0; seg--) {
         long long n0 = (long long)seg * a->k, n1 = n0 + a->k < a->nsteps ? n0 + a->k : a->nsteps;
@@ -531,10 +520,8 @@ extern "C" int kg_adjoint_gradient(kg_adjoint* a, kg_grad_result* out, double* d
             const double* phi_next = (n + 1 == n1) ? phi_end : tape_slot(a, (int)(n + 1 - n0)).f[KG_TAPE_PHI];
             double* l1 = a->lam + (size_t)lc * 3 * N;
             double* l0 = a->lam + (size_t)(lc ^ 1) * 3 * N;
-            kg_adj_pass_a<<<KG_ADJ_BLOCKS, KG_ADJ_THREADS, 0, a->stream>>>(a->adj, a->N, tp, phi_next, l1, l1 + N, w,
-                                                                           a->part);
-            kg_adj_pass_b<<<KG_ADJ_BLOCKS, KG_ADJ_THREADS, 0, a->stream>>>(a->adj, a->nx, a->ny, tp, l1 + 2 * N,
-                                                                           l0 + 2 * N, w, a->part);
+            kg_adj_pass_ab<<<KG_ADJ_BLOCKS, KG_ADJ_THREADS, 0, a->stream>>>(a->adj, a->nx, a->ny, tp, phi_next, l1,
+                                                                            l1 + N, l1 + 2 * N, l0 + 2 * N, w, a->part);
             kg_adj_pass_c<<<KG_ADJ_BLOCKS, KG_ADJ_THREADS, 0, a->stream>>>(a->adj, a->nx, a->ny, w, l0, l0 + N);
             lc ^= 1;
         }

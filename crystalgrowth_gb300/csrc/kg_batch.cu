@@ -136,9 +136,16 @@ struct kg_batch {
     cudaStream_t stream = nullptr;
     int cur = 0;
     long long steps = 0;
-    kg_batch_tuning tune{128, 64, KG_BATCH_LAUNCH, 100};
+    kg_batch_tuning tune{128, 64, KG_BATCH_LAUNCH, 100, 1};
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long cells = 0;
+    /* launch mode with tune.streams > 1: the instances are split into groups of about equal cell
+     * counts, each advanced on its own stream, so one group's next step overlaps another's tail */
+    int ngroups = 1;
+    int goff[KG_BATCH_MAX_STREAMS + 1] = {0};
+    cudaStream_t gs[KG_BATCH_MAX_STREAMS] = {nullptr};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[KG_BATCH_MAX_STREAMS] = {nullptr};
 };
 
 static void batch_drop_graphs(kg_batch* b)
@@ -167,6 +174,8 @@ static int valid_tuning(const kg_batch_tuning* t)
         return kg_fail(KG_ERR_INVALID, "batch tuning: unknown mode");
     if (t->chunk < 1 || t->chunk > 100000)
         return kg_fail(KG_ERR_INVALID, "batch tuning: chunk must lie in [1, 100000]");
+    if (t->streams < 1 || t->streams > KG_BATCH_MAX_STREAMS)
+        return kg_fail(KG_ERR_INVALID, "batch tuning: streams must lie in [1, %d]", KG_BATCH_MAX_STREAMS);
     return KG_OK;
 }
 
@@ -176,17 +185,40 @@ static int build_work(kg_batch* b)
     std::vector<int> order(b->n);
     for (int k = 0; k < b->n; k++)
         order[k] = k;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-        return (long long)b->inst[x].nx * b->inst[x].ny > (long long)b->inst[y].nx * b->inst[y].ny;
-    });
+    auto cells = [&](int k) { return (long long)b->inst[k].nx * b->inst[k].ny; };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells(x) > cells(y); });
+    /* groups of about equal total cells (largest instance to the lightest group first) */
+    int ng = b->tune.mode == KG_BATCH_LAUNCH ? b->tune.streams : 1;
+    if (ng > b->n)
+        ng = b->n;
+    std::vector<std::vector<int>> groups(ng);
+    std::vector<long long> load(ng, 0);
+    for (int k : order) {
+        int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        groups[g].push_back(k);
+        load[g] += cells(k);
+    }
     std::vector<int4> w;
     const int cw = b->tune.nt - 2;
-    for (int k : order) {
-        const KgInst& in = b->inst[k];
-        for (int j0 = 0; j0 < in.ny; j0 += b->tune.bh)
-            for (int i0 = 0; i0 < in.nx; i0 += cw)
-                w.push_back(make_int4(k, i0, j0, 0));
+    for (int g = 0; g < ng; g++) {
+        b->goff[g] = (int)w.size();
+        for (int k : groups[g]) {
+            const KgInst& in = b->inst[k];
+            for (int j0 = 0; j0 < in.ny; j0 += b->tune.bh)
+                for (int i0 = 0; i0 < in.nx; i0 += cw)
+                    w.push_back(make_int4(k, i0, j0, 0));
+        }
     }
+    b->goff[ng] = (int)w.size();
+    b->ngroups = ng;
+    for (int g = 0; g < ng && ng > 1; g++) {
+        if (!b->gs[g])
+            KG_CUDA(cudaStreamCreateWithFlags(&b->gs[g], cudaStreamNonBlocking));
+        if (!b->join_ev[g])
+            KG_CUDA(cudaEventCreateWithFlags(&b->join_ev[g], cudaEventDisableTiming));
+    }
+    if (ng > 1 && !b->fork_ev)
+        KG_CUDA(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
     if (b->d_work)
         cudaFree(b->d_work);
     b->d_work = nullptr;
@@ -197,21 +229,45 @@ static int build_work(kg_batch* b)
 }
 
 template <int NT>
-static cudaError_t launch_one(kg_batch* b, int from)
+static cudaError_t launch_range(kg_batch* b, int first, int count, int from, cudaStream_t st)
 {
-    kg_batch_step_kernel<NT><<<b->nwork, NT, 0, b->stream>>>(b->d_work, b->d_params, b->d_inst, b->arena, from,
-                                                            b->tune.bh);
+    kg_batch_step_kernel<NT><<<count, NT, 0, st>>>(b->d_work + first, b->d_params, b->d_inst, b->arena, from,
+                                                   b->tune.bh);
     return cudaGetLastError();
 }
 
-static int batch_launch_step(kg_batch* b, int from)
+static cudaError_t launch_group(kg_batch* b, int g, int from, cudaStream_t st)
 {
-    cudaError_t e;
+    int first = b->goff[g], count = b->goff[g + 1] - b->goff[g];
+    if (count <= 0)
+        return cudaSuccess;
     switch (b->tune.nt) {
-    case 32: e = launch_one<32>(b, from); break;
-    case 64: e = launch_one<64>(b, from); break;
-    case 256: e = launch_one<256>(b, from); break;
-    default: e = launch_one<128>(b, from); break;
+    case 32: return launch_range<32>(b, first, count, from, st);
+    case 64: return launch_range<64>(b, first, count, from, st);
+    case 256: return launch_range<256>(b, first, count, from, st);
+    default: return launch_range<128>(b, first, count, from, st);
+    }
+}
+
+/* nsteps consecutive steps from copy `from`: on the handle's stream, or forked
+ * over the group streams and joined back onto it */
+static int batch_launch_steps(kg_batch* b, int from, int nsteps)
+{
+    cudaError_t e = cudaSuccess;
+    if (b->ngroups <= 1) {
+        for (int s = 0; s < nsteps && e == cudaSuccess; s++)
+            e = launch_group(b, 0, from ^ (s & 1), b->stream);
+    } else {
+        e = cudaEventRecord(b->fork_ev, b->stream);
+        for (int g = 0; g < b->ngroups && e == cudaSuccess; g++) {
+            e = cudaStreamWaitEvent(b->gs[g], b->fork_ev, 0);
+            for (int s = 0; s < nsteps && e == cudaSuccess; s++)
+                e = launch_group(b, g, from ^ (s & 1), b->gs[g]);
+            if (e == cudaSuccess)
+                e = cudaEventRecord(b->join_ev[g], b->gs[g]);
+            if (e == cudaSuccess)
+                e = cudaStreamWaitEvent(b->stream, b->join_ev[g], 0);
+        }
     }
     if (e != cudaSuccess)
         return kg_cuda_fail(e, "kg_batch_step_kernel launch");
@@ -253,11 +309,7 @@ static int batch_build_graph(kg_batch* b, int from)
 {
     cudaGraph_t g = nullptr;
     KG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = KG_OK, c = from;
-    for (int s = 0; s < b->tune.chunk && rc == KG_OK; s++) {
-        rc = batch_launch_step(b, c);
-        c ^= 1;
-    }
+    int rc = batch_launch_steps(b, from, b->tune.chunk);
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc != KG_OK) {
         if (g)
@@ -320,12 +372,12 @@ extern "C" int kg_batch_step(kg_batch* b, long long nsteps)
         b->steps += b->tune.chunk;
         nsteps -= b->tune.chunk;
     }
-    for (; nsteps > 0; nsteps--) {
-        rc = batch_launch_step(b, b->cur);
+    if (nsteps > 0) {
+        rc = batch_launch_steps(b, b->cur, (int)nsteps);
         if (rc)
             return rc;
-        b->cur ^= 1;
-        b->steps++;
+        b->cur ^= (int)(nsteps & 1);
+        b->steps += nsteps;
     }
     return KG_OK;
 }
@@ -342,6 +394,14 @@ extern "C" int kg_batch_destroy(kg_batch* b)
     cudaFree(b->d_inst);
     cudaFree(b->d_work);
     cudaFree(b->d_bar);
+    for (int g = 0; g < KG_BATCH_MAX_STREAMS; g++) {
+        if (b->gs[g])
+            cudaStreamDestroy(b->gs[g]);
+        if (b->join_ev[g])
+            cudaEventDestroy(b->join_ev[g]);
+    }
+    if (b->fork_ev)
+        cudaEventDestroy(b->fork_ev);
     if (b->stream)
         cudaStreamDestroy(b->stream);
     delete b;
@@ -503,7 +563,8 @@ extern "C" int kg_batch_set_tuning(kg_batch* b, const kg_batch_tuning* t)
     if (rc)
         return rc;
     KG_CUDA(cudaStreamSynchronize(b->stream));
-    bool rework = t->nt != b->tune.nt || t->bh != b->tune.bh;
+    bool rework = t->nt != b->tune.nt || t->bh != b->tune.bh || t->streams != b->tune.streams ||
+                  t->mode != b->tune.mode;
     b->tune = *t;
     batch_drop_graphs(b);
     if (rework)
@@ -574,12 +635,14 @@ extern "C" int kg_batch_autotune(kg_batch* b, int trial_steps, kg_batch_tuning* 
         return kg_cuda_fail(e, "kg_batch_autotune setup");
     }
     const int nts[3] = {32, 64, 128};
-    const int bhs[4] = {8, 16, 32, 64};
-    const int modes[2] = {KG_BATCH_LAUNCH, KG_BATCH_PERSISTENT};
-    for (int mi = 0; mi < 2 && rc == KG_OK; mi++)
+    const int bhs[4] = {4, 8, 16, 32};
+    /* (mode, streams): one launch per step; the same over 4, 8 or 16 group streams; persistent */
+    const int modes[5][2] = {{KG_BATCH_LAUNCH, 1}, {KG_BATCH_LAUNCH, 4}, {KG_BATCH_LAUNCH, 8}, {KG_BATCH_LAUNCH, 16},
+                             {KG_BATCH_PERSISTENT, 1}};
+    for (int mi = 0; mi < 5 && rc == KG_OK; mi++)
         for (int ni = 0; ni < 3 && rc == KG_OK; ni++)
             for (int hi = 0; hi < 4 && rc == KG_OK; hi++) {
-                kg_batch_tuning t{nts[ni], bhs[hi], modes[mi], trial_steps};
+                kg_batch_tuning t{nts[ni], bhs[hi], modes[mi][0], trial_steps, modes[mi][1]};
                 rc = kg_batch_set_tuning(b, &t);
                 if (rc)
                     break;

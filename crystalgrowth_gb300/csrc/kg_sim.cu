@@ -14,8 +14,18 @@
 #include "kobayashi_color.h"
 
 
+/* resident CTAs per SM the register allocation must allow (0: the compiler's choice) */
+#ifndef KG_MIN_CTAS
+#define KG_MIN_CTAS 0
+#endif
+#if KG_MIN_CTAS > 0
+#define KG_STEP_BOUNDS(NT) __launch_bounds__(NT, KG_MIN_CTAS * 128 / NT)
+#else
+#define KG_STEP_BOUNDS(NT) __launch_bounds__(NT)
+#endif
+
 template <int NT>
-__global__ void __launch_bounds__(NT) kg_step_kernel(const __grid_constant__ KgDev P, int nx, int ny, int bh,
+__global__ void KG_STEP_BOUNDS(NT) kg_step_kernel(const __grid_constant__ KgDev P, int nx, int ny, int bh,
                                                      const double* __restrict__ phi_in, const double* __restrict__ t_in,
                                                      const double* __restrict__ th_in, double* __restrict__ phi_out,
                                                      double* __restrict__ t_out, double* __restrict__ th_out)

@@ -17,6 +17,7 @@ extern "C" {
 #endif
 
 #define KG_BATCH_LAUNCH 0      /* one kernel per step over all strips, CUDA-graph chunks */
+#define KG_BATCH_MAX_STREAMS 16
 #define KG_BATCH_PERSISTENT 1  /* one cooperative kernel per chunk, bounded grid barrier between steps */
 
 typedef struct kg_batch_tuning {
@@ -24,6 +25,8 @@ typedef struct kg_batch_tuning {
     int bh;     /* rows per strip */
     int mode;   /* KG_BATCH_LAUNCH or KG_BATCH_PERSISTENT */
     int chunk;  /* steps per graph (launch mode) or per persistent launch */
+    int streams; /* launch mode: instances split into this many groups of about equal cells, each
+                    group stepped on its own stream (1..KG_BATCH_MAX_STREAMS); 1 in persistent mode */
 } kg_batch_tuning;
 
 typedef struct kg_batch kg_batch;

@@ -123,6 +123,8 @@ def test_batch_rejects_bad_input():
     b = Batch([(8, 8)], [dict()])
     with pytest.raises(_lib.KgError):
         b.set_tuning(nt=100)
+    with pytest.raises(_lib.KgError):
+        b.set_tuning(streams=17)
     assert _lib.lib().kg_batch_get_fields(b._h, 3, None, None, None) == _lib.KG_ERR_INVALID
     assert b"out of range" in _lib.lib().kg_last_error()
     b.close()
@@ -142,5 +144,20 @@ def test_ensemble_512_full_length_sample():
         ref = ko_oracle.port_run(*configs.initial_fields(inst[k]["nx"], inst[k]["ny"], inst[k]["disks"]),
                                  inst[k]["params"], cfg["steps"], threads=16)
         for x, y in zip(b.fields(k), ref):
+            assert bits_equal(x, y), k
+    b.close()
+
+
+@pytest.mark.parametrize("streams,chunk", [(2, 7), (3, 100), (5, 4), (16, 1)])
+def test_batch_group_streams_bitwise(streams, chunk):
+    """instances split over several streams (each group steps on its own): same bits as the oracle"""
+    inst = small_ensemble(count=17, seed=9)
+    steps = 23
+    b = make_batch(inst)
+    b.set_tuning(nt=64, bh=8, mode=KG_BATCH_LAUNCH, chunk=chunk, streams=streams)
+    b.step(steps)
+    ref = oracle(inst, steps)
+    for k in range(len(inst)):
+        for x, y in zip(b.fields(k), ref[k]):
             assert bits_equal(x, y), k
     b.close()
