@@ -104,7 +104,10 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
         double s = (gx_neg ? KG_PI : 2.0 * KG_PI) + at;
         theta = (gx_neg || gy_neg) ? s : at;
     }
-    double arg = P.aniso * (theta - P.theta0);
+    /* theta == +0 (every cell the front has not reached) gives arg0 exactly; skip the two FP64 ops */
+    double arg = P.arg0;
+    if (kg_bits(theta) != 0)
+        arg = P.aniso * (theta - P.theta0);
     double e2, ee;
     if (kg_bits(arg) == kg_bits(P.arg0)) {
         e2 = P.e2_0;
