@@ -82,6 +82,7 @@ _SIGS = {
     "kg_version": [],
     "kg_diag_eval": [ctypes.c_int, _dp, _dp, ctypes.c_longlong, ctypes.c_double],
     "kg_diag_barrier_timeout": [ctypes.c_int, ctypes.c_longlong, _ip],
+    "kg_diag_mbar_timeout": [_ip],
     "kg_batch_create": [ctypes.c_int, _ip, _ip, ctypes.POINTER(Params), ctypes.POINTER(_vp)],
     "kg_batch_destroy": [_vp],
     "kg_batch_seed_disks": [_vp, ctypes.c_int, ctypes.c_int, _ip, _ip, _ip],

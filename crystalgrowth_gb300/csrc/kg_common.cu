@@ -19,6 +19,9 @@ int kg_fail(int code, const char* fmt, ...)
 
 int kg_cuda_fail(cudaError_t e, const char* what)
 {
+    /* the error is handled here: clear it from the runtime's per-thread last error, or the next
+     * launch check (cudaGetLastError) would report it again (a failed cudaMalloc leaves it there) */
+    (void)cudaGetLastError();
     return kg_fail(e == cudaErrorMemoryAllocation ? KG_ERR_NOMEM : KG_ERR_CUDA, "%s: %s (%s)", what,
                    cudaGetErrorString(e), cudaGetErrorName(e));
 }
@@ -174,6 +177,7 @@ int kg_prepare(const kg_params* p, KgDev* d)
     /* memo for T == 0 */
     d->u0 = p->gamma * (p->teq - 0.0);
     d->m0 = d->a_pi * kg_atan(d->u0);
+    d->t_small = kg_absorb_bound(p->teq);
     return KG_OK;
 }
 

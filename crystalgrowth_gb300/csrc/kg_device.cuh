@@ -22,7 +22,10 @@
  *     reached) come from a table computed once on the host with the same
  *     kg_sincos, keyed on the exact bits of the sine/cosine argument;
  *   - m = alpha/pi atan(gamma (Teq - T)) for the far-field argument
- *     gamma*Teq likewise.
+ *     gamma*Teq likewise; where |T| is small enough that Teq - T rounds to
+ *     Teq (a bound from the host), the argument itself is not computed;
+ *   - the Laplacians' 2 (E+W+N+S) + NE is one FMA: 2 x is exact, so the
+ *     reference's two roundings are the FMA's one (kg_twice_plus).
  * Comparisons use the bit patterns (integer pipe), never the FP64 pipe.
  */
 #pragma once
@@ -40,6 +43,7 @@ struct KgDev {
     double s0, c0;    /* sin(arg0), cos(arg0) */
     double eps0, epsd0, e2_0, ee0; /* eps, eps', eps^2, eps eps' at arg0 */
     double u0, m0;    /* gamma (Teq - 0) and (alpha/pi) atan(u0) */
+    uint64_t t_small; /* |T| bit patterns up to this leave Teq - T == Teq, so u == u0 */
 };
 
 #define KG_ABS_MASK 0x7fffffffffffffffull
@@ -142,6 +146,10 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
 #ifndef KG_EMU
 #define KG_EMU 0
 #endif
+/* 1: kg_twice_plus in the Laplacians and the T bound for m (both exact); 0: the plain sequence */
+#ifndef KG_FUSE
+#define KG_FUSE 1
+#endif
 
 /* 9-point Laplacian in the reference's summation order (src/Kobayashi.cpp:142-151). */
 __device__ __forceinline__ double kg_lap(const KgDev& P, double c, double e, double w, double n, double s, double ne,
@@ -153,6 +161,8 @@ __device__ __forceinline__ double kg_lap(const KgDev& P, double c, double e, dou
     v = kg_iadd(kg_iadd(kg_iadd(kg_iadd(kg_imul2(s4), ne), sw), nw), se) - 12.0 * c;
 #elif KG_EMU == 1
     v = kg_imul2(e + w + n + s) + ne + sw + nw + se - 12.0 * c;
+#elif KG_FUSE
+    v = kg_twice_plus(e + w + n + s, ne) + sw + nw + se - 12.0 * c;
 #else
     v = 2.0 * (e + w + n + s) + ne + sw + nw + se - 12.0 * c;
 #endif
@@ -173,8 +183,15 @@ __device__ __forceinline__ void kg_stage2(const KgDev& P, double e2c, double gx,
     double term1 = kg_idiv(aN - aS, &P.idy);
     double term2 = -kg_idiv(bE - bW, &P.idx);
     double term3 = gex * gx + gey * gy;
-    double u = P.gamma * (P.teq - t);
-    double m = (kg_bits(u) == kg_bits(P.u0)) ? P.m0 : P.a_pi * kg_atan(u);
+    double m = P.m0;
+#if KG_FUSE
+    if ((kg_bits(t) & KG_ABS_MASK) > P.t_small)
+#endif
+    {
+        double u = P.gamma * (P.teq - t);
+        if (kg_bits(u) != kg_bits(P.u0))
+            m = P.a_pi * kg_atan(u);
+    }
     double old_phi = phi;
     double old_t = t;
     double rhs = term1 + term2 + e2c * lap_phi + term3 + old_phi * (1.0 - old_phi) * (old_phi - 0.5 + m);
@@ -202,56 +219,193 @@ __device__ __forceinline__ int kg_wrap(int i, int n)
  * Shared memory: phi ring 8 x (NT+2), T ring 4 x NT, e2/b ring 2 x 2 x NT.
  */
 template <int NT>
-struct KgSmem {
-    double phi[8][NT + 2];
-    double t[4][NT];
+struct __align__(16) KgSmem {
+    double phi[8][NT + 2]; /* column i0-2+k at [.][k]; rows by local index (row - (j0-2)) & 7 */
+    double t[8][NT + 2];   /* same layout as phi */
     double e2[2][NT];
     double b[2][NT];
+    unsigned long long mbar[16]; /* bulk-copy completion: [0..7] phi slots, [8..15] T slots */
 };
 
+/* ---- bulk (TMA) row copies into shared memory, completion tracked by mbarriers ---- */
+
+__device__ __forceinline__ unsigned kg_smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void kg_mbar_init(unsigned long long* mbar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(kg_smem_addr(mbar)), "r"(count) : "memory");
+}
+
+/* one arrival that also announces `bytes` of transaction data */
+__device__ __forceinline__ void kg_mbar_expect(unsigned long long* mbar, unsigned bytes)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\t"
+                 "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(kg_smem_addr(mbar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool kg_mbar_test(unsigned long long* mbar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(kg_smem_addr(mbar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+/* a bounded wait for phase `parity` of an mbarrier: about 0.7 s at most, then
+ * the error flag is raised and false returned (nothing here waits forever) */
+__device__ __forceinline__ bool kg_mbar_wait(unsigned long long* mbar, unsigned parity, unsigned* err)
+{
+    for (int i = 0; i < (1 << 24); i++) {
+        if (kg_mbar_test(mbar, parity))
+            return true;
+        __nanosleep(32);
+    }
+    if (err)
+        atomicExch(err, 1u);
+    return false;
+}
+
+/* bytes (a multiple of 16) from 16-byte aligned global src to 16-byte aligned shared dst */
+__device__ __forceinline__ void kg_bulk_copy(void* dst, const void* src, unsigned bytes, unsigned long long* mbar)
+{
+    unsigned long long gsrc;
+    asm volatile("cvta.to.global.u64 %0, %1;" : "=l"(gsrc) : "l"(src));
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     kg_smem_addr(dst)),
+                 "l"(gsrc), "r"(bytes), "r"(kg_smem_addr(mbar))
+                 : "memory");
+}
+
+/*
+ * The marching strip: one CTA of NT threads advances columns [i0, i0+NT-2)
+ * (clipped to nx) and rows [j0, j0+bh) (clipped to ny) of one grid by one
+ * step, reading (phi, T, theta) from `*_in` and writing `*_out`.
+ *
+ * Rows of phi and T reach shared memory in one of two ways.  With `tma`
+ * (strips that do not wrap around the grid's left/right edge, nx even so
+ * that every row starts 16-byte aligned) one thread issues a bulk copy of
+ * each row segment, columns i0-2 .. i0+NT-1, one row ahead of use, and the
+ * CTA waits on that row's mbarrier; otherwise every lane loads its own
+ * column (wrapped).  Ring slots are indexed by the row's position in the
+ * strip, (row - (j0-2)) & 7.  `err` (may be null) receives a time-out of a
+ * bulk-copy wait.
+ */
 template <int NT, bool TAPE = false>
 __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const double* __restrict__ phi_in,
                                          const double* __restrict__ t_in, const double* __restrict__ th_in,
                                          double* __restrict__ phi_out, double* __restrict__ t_out,
                                          double* __restrict__ th_out, int i0, int j0, int bh, KgSmem<NT>& sm,
-                                         const KgTape* tape = nullptr)
+                                         const KgTape* tape = nullptr, bool tma = false, unsigned* err = nullptr)
 {
     const int L = threadIdx.x;
     const int jend = min(j0 + bh, ny);
-    /* columns: phi smem index k <-> column i0-2+k; lane L <-> column i0-1+L */
+    const int base = j0 - 2; /* row of ring slot index 0 */
+    /* columns: smem index k <-> column i0-2+k; lane L <-> column i0-1+L <-> index L+1 */
     const int colA = kg_wrap(i0 - 2 + L, nx);
     const int colB = (L < 2) ? kg_wrap(i0 - 2 + NT + L, nx) : 0;
     const int col = kg_wrap(i0 - 1 + L, nx);
     const bool out_lane = (L >= 1) && (L <= NT - 2) && (i0 - 1 + L < nx);
+    const unsigned row_bytes = (NT + 2) * sizeof(double);
 
     auto load_phi_row = [&](int q) {
         const double* row = phi_in + (size_t)kg_wrap(q, ny) * nx;
-        sm.phi[q & 7][L] = row[colA];
+        sm.phi[(q - base) & 7][L] = row[colA];
         if (L < 2)
-            sm.phi[q & 7][NT + L] = row[colB];
+            sm.phi[(q - base) & 7][NT + L] = row[colB];
     };
-    /* rows j0-2 and j0-1 of phi before the march */
-    load_phi_row(j0 - 2);
-    load_phi_row(j0 - 1);
+    /* mbarriers count each ring's rows from the ring's first row (phi: j0-2, T: j0-1), so that the
+     * k-th arrival at a barrier is its phase k: row q waits on phase (q - first) >> 3 */
+    auto phi_bar = [&](int q) { return &sm.mbar[(q - base) & 7]; };
+    auto phi_par = [&](int q) { return (unsigned)((q - base) >> 3) & 1u; };
+    auto t_bar = [&](int q) { return &sm.mbar[8 + ((q - j0 + 1) & 7)]; };
+    auto t_par = [&](int q) { return (unsigned)((q - j0 + 1) >> 3) & 1u; };
+    auto issue_phi = [&](int q) {
+        unsigned long long* mb = phi_bar(q);
+        kg_mbar_expect(mb, row_bytes);
+        kg_bulk_copy(sm.phi[(q - base) & 7], phi_in + (size_t)kg_wrap(q, ny) * nx + (i0 - 2), row_bytes, mb);
+    };
+    auto issue_t = [&](int q) {
+        unsigned long long* mb = t_bar(q);
+        kg_mbar_expect(mb, row_bytes);
+        kg_bulk_copy(sm.t[(q - base) & 7], t_in + (size_t)kg_wrap(q, ny) * nx + (i0 - 2), row_bytes, mb);
+    };
+    bool ok = true;
+    int r_fail = jend + 1;
+    auto wait_phi = [&](int q) {
+        if (!kg_mbar_wait(phi_bar(q), phi_par(q), err))
+            ok = false;
+    };
+    auto wait_t = [&](int q) {
+        if (!kg_mbar_wait(t_bar(q), t_par(q), err))
+            ok = false;
+    };
+
+    if (tma) {
+        if (L == 0) {
+            for (int k = 0; k < 16; k++)
+                kg_mbar_init(&sm.mbar[k], 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (L == 0) {
+            issue_phi(j0 - 2);
+            issue_phi(j0 - 1);
+            issue_phi(j0);
+            issue_t(j0 - 1);
+        }
+        /* the march waits for row r+1 at row r; the two rows above the strip are waited for here */
+        wait_phi(j0 - 2);
+        wait_phi(j0 - 1);
+    } else {
+        /* rows j0-2 and j0-1 of phi before the march */
+        load_phi_row(j0 - 2);
+        load_phi_row(j0 - 1);
+    }
 
     /* registers: stage-1 results of this lane's column for rows r-2, r-1, r */
     double e2_m2 = 0, a_m2 = 0;
     double e2_m1 = 0, a_m1 = 0, gx_m1 = 0, gy_m1 = 0;
     for (int r = j0 - 1; r <= jend; r++) {
-        /* loads: phi row r+1, T row r, theta of this lane at row r */
-        load_phi_row(r + 1);
         const size_t roff = (size_t)kg_wrap(r, ny) * nx;
-        sm.t[r & 3][L] = t_in[roff + col];
+        if (tma) {
+            /* prefetch phi row r+2 and T row r+1, then wait for phi row r+1 and T row r */
+            if (L == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                if (r + 2 <= jend + 1)
+                    issue_phi(r + 2);
+                if (r + 1 <= jend)
+                    issue_t(r + 1);
+            }
+            wait_phi(r + 1);
+            wait_t(r);
+        } else {
+            /* loads: phi row r+1, T row r */
+            load_phi_row(r + 1);
+            sm.t[(r - base) & 7][L + 1] = t_in[roff + col];
+        }
         double theta = th_in[roff + col];
-        /* a one-warp strip (NT = 32) needs no CTA barrier: warps never wait on each other */
-        if constexpr (NT == 32)
+        /* the row barrier, which also makes a bulk-copy time-out a CTA-wide decision (a one-warp
+         * strip, NT = 32, needs only a warp vote: warps never wait on each other) */
+        bool fail;
+        if constexpr (NT == 32) {
             __syncwarp();
-        else
-            __syncthreads();
+            fail = __any_sync(0xffffffffu, !ok);
+        } else
+            fail = __syncthreads_or(!ok) != 0;
+        if (fail) {
+            r_fail = r;
+            break;
+        }
 
+        const int rm = (r - 1 - base) & 7, r0 = (r - base) & 7, rp = (r + 1 - base) & 7;
         /* stage 1 at row r for all NT lanes */
-        KgS1 s1 = kg_stage1(P, sm.phi[r & 7][L + 2], sm.phi[r & 7][L], sm.phi[(r + 1) & 7][L + 1],
-                            sm.phi[(r - 1) & 7][L + 1], theta);
+        KgS1 s1 = kg_stage1(P, sm.phi[r0][L + 2], sm.phi[r0][L], sm.phi[rp][L + 1], sm.phi[rm][L + 1], theta);
         sm.e2[r & 1][L] = s1.e2;
         sm.b[r & 1][L] = s1.b;
         if (out_lane && r >= j0 && r < jend) {
@@ -267,16 +421,15 @@ __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const d
         /* stage 2 at row s = r-1 for the output lanes */
         const int s = r - 1;
         if (out_lane && s >= j0) {
-            const int sm1 = (s - 1) & 7, s0 = s & 7, sp1 = (s + 1) & 7;
+            const int sm1 = (s - 1 - base) & 7, s0 = (s - base) & 7, sp1 = (s + 1 - base) & 7;
             const int k = L + 1;
             double lap_phi = kg_lap(P, sm.phi[s0][k], sm.phi[s0][k + 1], sm.phi[s0][k - 1], sm.phi[sp1][k],
                                     sm.phi[sm1][k], sm.phi[sp1][k + 1], sm.phi[sm1][k - 1], sm.phi[sp1][k - 1],
                                     sm.phi[sm1][k + 1]);
-            const int t0 = s & 3, tm = (s - 1) & 3, tp = (s + 1) & 3;
-            double lap_t = kg_lap(P, sm.t[t0][L], sm.t[t0][L + 1], sm.t[t0][L - 1], sm.t[tp][L], sm.t[tm][L],
-                                  sm.t[tp][L + 1], sm.t[tm][L - 1], sm.t[tp][L - 1], sm.t[tm][L + 1]);
+            double lap_t = kg_lap(P, sm.t[s0][k], sm.t[s0][k + 1], sm.t[s0][k - 1], sm.t[sp1][k], sm.t[sm1][k],
+                                  sm.t[sp1][k + 1], sm.t[sm1][k - 1], sm.t[sp1][k - 1], sm.t[sm1][k + 1]);
             double phi = sm.phi[s0][k];
-            double t = sm.t[t0][L];
+            double t = sm.t[s0][k];
             const size_t soff = (size_t)kg_wrap(s, ny) * nx;
             if constexpr (TAPE) {
                 KgS2Aux aux;
@@ -303,5 +456,15 @@ __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const d
         a_m1 = s1.a;
         gx_m1 = s1.gx;
         gy_m1 = s1.gy;
+    }
+    if (tma && r_fail <= jend && L == 0) {
+        /* a wait ran out: before the CTA leaves (its shared memory goes to the next CTA), give the
+         * bulk copies still in flight -- at most the last 8 rows issued per ring -- a second bounded
+         * wait */
+        const int last_phi = min(r_fail + 2, jend + 1), last_t = min(r_fail + 1, jend);
+        for (int q = max(j0 - 2, last_phi - 7); q <= last_phi; q++)
+            kg_mbar_wait(phi_bar(q), phi_par(q), nullptr);
+        for (int q = max(j0 - 1, last_t - 7); q <= last_t; q++)
+            kg_mbar_wait(t_bar(q), t_par(q), nullptr);
     }
 }

@@ -31,6 +31,10 @@ __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double
             r = __dmul_rn(2.0, v);
         } else if (fn == KG_FN_DIV) {
             r = v / b;
+        } else if (fn == KG_FN_TWICE_PLUS) {
+            r = kg_twice_plus(v, x[n - 1 - i]);
+        } else if (fn == KG_FN_MUL2_ADD) {
+            r = __dadd_rn(__dmul_rn(2.0, v), x[n - 1 - i]);
         }
         y[i] = r;
     }
@@ -38,7 +42,7 @@ __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double
 
 extern "C" int kg_diag_eval(int fn, const double* x, double* y, long long n, double b)
 {
-    if (fn < KG_FN_ATAN || fn > KG_FN_MUL2 || n < 0 || (n > 0 && (!x || !y)))
+    if (fn < KG_FN_ATAN || fn > KG_FN_MUL2_ADD || n < 0 || (n > 0 && (!x || !y)))
         return kg_fail(KG_ERR_INVALID, "kg_diag_eval: bad arguments");
     double yh = 0, yl = 0;
     kg_idivc ic;
@@ -116,5 +120,39 @@ extern "C" int kg_diag_fp64_peak(double* ops_per_s)
     if (e != cudaSuccess)
         return kg_cuda_fail(e, "kg_diag_fp64_peak");
     *ops_per_s = (double)blocks * threads * KG_PEAK_ITERS * KG_PEAK_CHAINS / (best * 1e-3);
+    return KG_OK;
+}
+
+/* An mbarrier that no copy ever completes: the strip kernel's bounded wait
+ * must give up, raise the flag and return. */
+__global__ void kg_diag_mbar_kernel(unsigned* err)
+{
+    __shared__ unsigned long long mbar;
+    if (threadIdx.x == 0) {
+        kg_mbar_init(&mbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    kg_mbar_wait(&mbar, 0, err);
+}
+
+extern "C" int kg_diag_mbar_timeout(int* timed_out)
+{
+    if (!timed_out)
+        return kg_fail(KG_ERR_INVALID, "kg_diag_mbar_timeout: null pointer");
+    unsigned* d = nullptr;
+    KG_CUDA(cudaMalloc(&d, sizeof(unsigned)));
+    cudaError_t e = cudaMemset(d, 0, sizeof(unsigned));
+    if (e == cudaSuccess) {
+        kg_diag_mbar_kernel<<<1, 32>>>(d);
+        e = cudaGetLastError();
+    }
+    unsigned h = 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess)
+        return kg_cuda_fail(e, "kg_diag_mbar_timeout");
+    *timed_out = h != 0;
     return KG_OK;
 }

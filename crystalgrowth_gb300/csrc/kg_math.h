@@ -451,4 +451,41 @@ KG_HD double kg_imul2(double x)
     return kg_from_bits(u + 0x0010000000000000ull);
 }
 
+/* RN(RN(2 s) + y), the reference's "2.0 * s + y", in one FMA.  2 s is exact
+ * unless it overflows, so the two roundings reduce to the FMA's one.  The
+ * exception is |s| >= 2^1023 (exponent field 2046), where RN(2 s) = +-inf;
+ * that case is finished in integer arithmetic, with no FP64 instruction:
+ * inf + y = inf, except NaN for y = NaN or y = -inf of the other sign. */
+KG_HD double kg_twice_plus(double s, double y)
+{
+    uint64_t u = kg_bits(s);
+    if ((u & 0x7ff0000000000000ull) != 0x7fe0000000000000ull)
+        return kg_fma(2.0, s, y);
+    uint64_t inf = (u & 0x8000000000000000ull) | 0x7ff0000000000000ull;
+    uint64_t v = kg_bits(y);
+    if ((v & 0x7fffffffffffffffull) > 0x7ff0000000000000ull)
+        return kg_from_bits(v | 0x0008000000000000ull);
+    if (v == (inf ^ 0x8000000000000000ull))
+        return kg_from_bits(0x7ff8000000000000ull);
+    return kg_from_bits(inf);
+}
+
+/* The largest |t| for which c - t rounds to c exactly, as a bit pattern of
+ * |t| (compare (bits(t) & ~sign) <= bound): 2^(e-55) for c normal in
+ * [2^e, 2^(e+1)), below half the spacing of the doubles next to c on either
+ * side; only t = +-0 for c zero or subnormal. */
+KG_HD uint64_t kg_absorb_bound(double c)
+{
+    uint64_t a = kg_bits(c) & 0x7fffffffffffffffull;
+    int e = (int)(a >> 52); /* biased exponent of c */
+    if (e == 0 || e == 0x7ff)
+        return 0;
+    int eb = e - 55; /* biased exponent of 2^(e-55) */
+    if (eb >= 1)
+        return (uint64_t)eb << 52;
+    if (eb > -52)
+        return 1ull << (51 + eb); /* a subnormal power of two */
+    return 0;
+}
+
 #endif /* KG_MATH_H */

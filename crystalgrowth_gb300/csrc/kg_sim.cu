@@ -24,15 +24,25 @@
 #define KG_STEP_BOUNDS(NT) __launch_bounds__(NT)
 #endif
 
+/* rows of phi and T reach shared memory by bulk (TMA) copies where the strip allows it (1), or by
+ * per-lane loads everywhere (0) */
+#ifndef KG_TMA
+#define KG_TMA 1
+#endif
+
 template <int NT>
 __global__ void KG_STEP_BOUNDS(NT) kg_step_kernel(const __grid_constant__ KgDev P, int nx, int ny, int bh,
                                                      const double* __restrict__ phi_in, const double* __restrict__ t_in,
                                                      const double* __restrict__ th_in, double* __restrict__ phi_out,
-                                                     double* __restrict__ t_out, double* __restrict__ th_out)
+                                                     double* __restrict__ t_out, double* __restrict__ th_out,
+                                                     unsigned* err)
 {
     __shared__ KgSmem<NT> sm;
-    kg_strip<NT>(P, nx, ny, phi_in, t_in, th_in, phi_out, t_out, th_out, blockIdx.x * (NT - 2), blockIdx.y * bh, bh,
-                 sm);
+    const int i0 = blockIdx.x * (NT - 2);
+    /* bulk copies need 16-byte aligned rows (nx even) and a strip that does not wrap left/right */
+    const bool tma = KG_TMA && (nx % 2 == 0) && i0 >= 2 && i0 + NT <= nx;
+    kg_strip<NT>(P, nx, ny, phi_in, t_in, th_in, phi_out, t_out, th_out, i0, blockIdx.y * bh, bh, sm, nullptr, tma,
+                 err);
 }
 
 struct kg_sim {
@@ -48,6 +58,7 @@ struct kg_sim {
     int nt = 128; /* threads per strip CTA (strip width nt - 2 columns) */
     int bh = 64;  /* rows per strip */
     float* color = nullptr; /* RGBA staging buffer for kg_colormap, allocated on first use */
+    unsigned* err = nullptr; /* raised by a kernel whose bounded wait ran out */
 };
 
 static void drop_graphs(kg_sim* h)
@@ -65,12 +76,14 @@ static int launch_step(kg_sim* h, int from)
     double* const* a = h->buf[from];
     double* const* b = h->buf[from ^ 1];
     if (h->nt == 32)
-        kg_step_kernel<32><<<grid, 32, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1], b[2]);
+        kg_step_kernel<32><<<grid, 32, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1], b[2],
+                                                        h->err);
     else if (h->nt == 64)
-        kg_step_kernel<64><<<grid, 64, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1], b[2]);
+        kg_step_kernel<64><<<grid, 64, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1], b[2],
+                                                        h->err);
     else
         kg_step_kernel<128><<<grid, 128, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1],
-                                                          b[2]);
+                                                          b[2], h->err);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return kg_cuda_fail(e, "kg_step_kernel launch");
@@ -125,6 +138,8 @@ extern "C" int kg_destroy(kg_sim* h)
                 cudaFree(h->buf[k][f]);
     if (h->color)
         cudaFree(h->color);
+    if (h->err)
+        cudaFree(h->err);
     if (h->stream)
         cudaStreamDestroy(h->stream);
     delete h;
@@ -179,6 +194,10 @@ extern "C" int kg_create(int nx, int ny, const kg_params* p, kg_sim** out)
     for (int k = 0; k < 2 && e == cudaSuccess; k++)
         for (int f = 0; f < 3 && e == cudaSuccess; f++)
             e = cudaMalloc(&h->buf[k][f], bytes);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&h->err, sizeof(unsigned));
+    if (e == cudaSuccess)
+        e = cudaMemset(h->err, 0, sizeof(unsigned));
     if (e != cudaSuccess) {
         rc = kg_cuda_fail(e, "kg_create: device allocation");
         kg_destroy(h);
@@ -298,13 +317,26 @@ extern "C" int kg_update(kg_sim* h)
     return KG_OK;
 }
 
+/* waits for the stream and reports (then clears) a bounded wait that ran out */
+static int sync_and_check(kg_sim* h)
+{
+    unsigned flag = 0;
+    KG_CUDA(cudaMemcpyAsync(&flag, h->err, sizeof flag, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(cudaStreamSynchronize(h->stream));
+    if (flag) {
+        cudaMemsetAsync(h->err, 0, sizeof(unsigned), h->stream);
+        cudaStreamSynchronize(h->stream);
+        return kg_fail(KG_ERR_TIMEOUT, "kg_step: a bulk-copy wait in the step kernel ran out; the state is unreliable");
+    }
+    return KG_OK;
+}
+
 extern "C" int kg_sync(kg_sim* h)
 {
     int rc = check(h);
     if (rc)
         return rc;
-    KG_CUDA(cudaStreamSynchronize(h->stream));
-    return KG_OK;
+    return sync_and_check(h);
 }
 
 extern "C" int kg_get_fields(kg_sim* h, double* phi, double* T, double* theta)
@@ -317,8 +349,7 @@ extern "C" int kg_get_fields(kg_sim* h, double* phi, double* T, double* theta)
     for (int f = 0; f < 3; f++)
         if (dst[f])
             KG_CUDA(cudaMemcpyAsync(dst[f], h->buf[h->cur][f], bytes, cudaMemcpyDeviceToHost, h->stream));
-    KG_CUDA(cudaStreamSynchronize(h->stream));
-    return KG_OK;
+    return sync_and_check(h);
 }
 
 extern "C" int kg_set_fields(kg_sim* h, const double* phi, const double* T, const double* theta)

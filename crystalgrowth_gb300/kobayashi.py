@@ -50,8 +50,18 @@ class Kobayashi:
         cx, cy, r = (np.ascontiguousarray(d[:, k]) for k in range(3))
         check(lib().kg_seed_disks(self._h, len(d), iptr(cx), iptr(cy), iptr(r)))
 
-    def fields(self):
-        out = [np.empty((self.ny, self.nx)) for _ in range(3)]
+    def fields(self, out=None):
+        """(phi, T, theta) as (ny, nx) float64 arrays.  `out`: three C-contiguous float64 arrays of
+        that shape to copy into (for example page-locked buffers, which the copy reaches at the
+        link's full speed); new arrays otherwise."""
+        if out is None:
+            out = [np.empty((self.ny, self.nx)) for _ in range(3)]
+        else:
+            out = list(out)
+            if len(out) != 3 or any(not isinstance(a, np.ndarray) or a.dtype != np.float64 or
+                                    a.size != self.nx * self.ny or not a.flags.c_contiguous or
+                                    not a.flags.writeable for a in out):
+                raise ValueError("out: three writeable C-contiguous float64 arrays of %d x %d" % (self.ny, self.nx))
         check(lib().kg_get_fields(self._h, *[dptr(a) for a in out]))
         return tuple(out)
 

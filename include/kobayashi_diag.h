@@ -23,6 +23,8 @@ extern "C" {
 #define KG_FN_ADD 7   /* y[i] = x[i] + x[n-1-i], the hardware addition */
 #define KG_FN_IMUL2 8 /* y = kg_imul2(x): 2 x by an exponent increment */
 #define KG_FN_MUL2 9  /* y = 2 x, the hardware multiplication */
+#define KG_FN_TWICE_PLUS 10 /* y[i] = kg_twice_plus(x[i], x[n-1-i]): 2 x + y in one FMA */
+#define KG_FN_MUL2_ADD 11   /* y[i] = 2 x[i] + x[n-1-i], two hardware roundings */
 
 /* Evaluates function `fn` on n host values on the current device (synchronous). */
 KG_API int kg_diag_eval(int fn, const double* x, double* y, long long n, double b);
@@ -31,6 +33,11 @@ KG_API int kg_diag_eval(int fn, const double* x, double* y, long long n, double 
  * waits for one CTA more: every wait must give up after max_polls polls.
  * *timed_out = 1 when the error flag was raised (the expected outcome). */
 KG_API int kg_diag_barrier_timeout(int blocks, long long max_polls, int* timed_out);
+
+/* Waits, with the strip kernel's bounded wait, on an mbarrier that no bulk
+ * copy completes: the wait must give up (about half a second) and raise the
+ * flag.  *timed_out = 1 is the expected outcome. */
+KG_API int kg_diag_mbar_timeout(int* timed_out);
 
 /* Measures the FP64 FMA throughput of the current device: lane-operations per second. */
 KG_API int kg_diag_fp64_peak(double* ops_per_s);

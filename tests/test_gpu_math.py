@@ -76,3 +76,22 @@ def test_integer_pipe_add_and_double_equal_hardware_on_device():
             assert (((a.view(np.uint64) == r.view(np.uint64)) | (np.isnan(a) & np.isnan(r))).all())
             a, r = dev_eval(8, x), dev_eval(9, x)
             assert (((a.view(np.uint64) == r.view(np.uint64)) | (np.isnan(a) & np.isnan(r))).all())
+
+
+def test_twice_plus_equals_two_roundings_on_device():
+    """kg_twice_plus(x, y) (one FMA, integer finish where 2 x overflows) == RN(RN(2 x) + y) on the device,
+    including |x| >= 2^1023, infinities and NaN"""
+    rng = np.random.default_rng(78)
+    n = 2_000_000
+    big = rng.uniform(1, 2, n) * 2.0 ** 1023 * rng.choice([-1, 1], n)
+    cases = [rng.standard_normal(n) * 10.0 ** rng.integers(-320, 308, n),
+             np.concatenate([rng.uniform(-1, 1, n), -2 * rng.uniform(-1, 1, n)[::-1]]),
+             np.concatenate([big, rng.standard_normal(n) * 10.0 ** rng.integers(300, 308, n)]),
+             np.concatenate([big[:8], [math.inf, -math.inf, math.nan, -1.7976931348623157e308, 1.7976931348623157e308,
+                                       0.0, -0.0, 5e-324]]),
+             np.array([2.0 ** 1023, 1.5 * 2.0 ** 1023, -2.0 ** 1023, math.inf, -math.inf, math.nan, 1.0,
+                       -math.inf, math.inf, -1.7976931348623157e308, math.inf, -math.inf])]
+    for x in cases:
+        with np.errstate(all="ignore"):
+            a, r = dev_eval(10, x), dev_eval(11, x)
+            assert (((a.view(np.uint64) == r.view(np.uint64)) | (np.isnan(a) & np.isnan(r))).all())

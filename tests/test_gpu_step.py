@@ -102,18 +102,21 @@ def test_graph_chunks_do_not_change_results():
             assert bits_equal(x, y)
 
 
-@pytest.mark.parametrize("nt,bh", [(32, 1), (32, 17), (64, 1), (64, 8), (128, 3), (128, 200)])
-def test_strip_shape_does_not_change_results(nt, bh):
+@pytest.mark.parametrize("nx", [141, 260])
+@pytest.mark.parametrize("nt,bh", [(32, 1), (32, 17), (64, 1), (64, 8), (64, 40), (128, 3), (128, 16), (128, 200)])
+def test_strip_shape_does_not_change_results(nx, nt, bh):
+    """odd width: every strip loads its columns lane by lane; even width (260): interior strips
+    stage their rows with bulk copies, across strip heights that wrap each 8-row ring several times"""
     p = dict(configs.BASE)
-    disks = [(70, 50, 6), (10, 90, 4)]
-    sim = Kobayashi(141, 103, p["dt"], params=p)
+    disks = [(70, 50, 6), (10, 90, 4), (nx - 20, 30, 5)]
+    sim = Kobayashi(nx, 103, p["dt"], params=p)
     sim.seed_disks(disks)
     sim.set_tile(nt, bh)
     assert sim.tile() == (nt, min(bh, 103))
     sim.step(90)
     a = sim.fields()
     sim.close()
-    b = oracle_run(141, 103, p, disks, 90)
+    b = oracle_run(nx, 103, p, disks, 90)
     for x, y in zip(a, b):
         assert bits_equal(x, y)
 
@@ -217,3 +220,29 @@ def test_translation_invariance_grid8192_1000_steps():
     assert np.abs(a[0]).max() > 0.5  # crystals have grown
     for x, y in zip(a, b):
         assert bits_equal(np.roll(x, (dj, di), axis=(0, 1)), y)
+
+
+def test_device_out_of_memory_is_an_error_not_a_crash():
+    """a grid larger than the GPU's memory: cudaMalloc fails, the call returns KG_ERR_NOMEM and the
+    library (and the CUDA context) stay usable"""
+    from crystalgrowth_gb300 import _lib
+    with pytest.raises(KgError) as e:
+        Kobayashi(131072, 131072, 1e-4)  # 2^34 cells: 824 GB of state
+    assert e.value.code == _lib.KG_ERR_NOMEM
+    sim = Kobayashi(32, 32, 1e-4)
+    sim.step(5)
+    sim.close()
+
+
+def test_bulk_copy_wait_runs_out_and_context_survives():
+    """the strip kernel's mbarrier wait is bounded: on a barrier nothing completes it gives up,
+    raises the flag, and the context stays usable"""
+    import ctypes
+    from crystalgrowth_gb300 import _lib
+    flag = ctypes.c_int(-1)
+    _lib.check(_lib.lib().kg_diag_mbar_timeout(ctypes.byref(flag)))
+    assert flag.value == 1
+    sim = Kobayashi(64, 64, 1e-4)
+    sim.step(3)
+    sim.sync()
+    sim.close()

@@ -161,3 +161,39 @@ def test_imul2_matches_hardware():
     for x in _pairs(22):
         with np.errstate(all="ignore"):
             assert _same(ko_oracle.kg_eval(8, x), ko_oracle.kg_eval(9, x))
+
+
+def test_twice_plus_equals_two_roundings():
+    """kg_twice_plus(x, y) == RN(RN(2 x) + y): one FMA where 2 x is exact, integers where it overflows"""
+    rng = np.random.default_rng(23)
+    n = 1_000_000
+    big = rng.uniform(1, 2, n) * 2.0 ** 1023 * rng.choice([-1, 1], n)
+    cases = _pairs(24) + [np.concatenate([big, rng.standard_normal(n) * 10.0 ** rng.integers(300, 308, n)]),
+                          np.array([2.0 ** 1023, -2.0 ** 1023, 1.5 * 2.0 ** 1023, math.inf, -math.inf, math.nan,
+                                    -math.inf, math.inf, -1.7976931348623157e308, 1.0, math.nan, -math.inf])]
+    for x in cases:
+        with np.errstate(all="ignore"):
+            assert _same(ko_oracle.kg_eval(10, x), ko_oracle.kg_eval(11, x))
+
+
+def test_absorb_bound():
+    """kg_absorb_bound(c): every |t| up to it leaves c - t == c (both signs of t and c), and it is
+    2^(e-55) for normal c in [2^e, 2^(e+1)); zero, subnormal and non-finite c give 0 (only t = +-0)"""
+    rng = np.random.default_rng(25)
+    c = np.concatenate([rng.uniform(0.5, 1.5, 20000), rng.uniform(-4, 4, 20000),
+                        rng.standard_normal(20000) * 10.0 ** rng.integers(-307, 307, 20000),
+                        [1.0, 2.0, 0.5, 2.0 ** -1022, 2.0 ** -1000, 2.0 ** -968, 2.0 ** -967, 1.7976931348623157e308,
+                         0.0, -0.0, 5e-324, math.inf, math.nan]])
+    bound = ko_oracle.kg_eval(12, c)
+    fin = np.isfinite(c) & (np.abs(c) >= 2.0 ** -1022)
+    assert not bound[~fin].any()
+    e = np.frexp(np.abs(c[fin]))[1] - 1  # c in [2^e, 2^(e+1))
+    with np.errstate(under="ignore"):
+        want = np.ldexp(1.0, (e - 55).astype(np.int64))
+    assert np.array_equal(bound[fin], want)
+    for s in (1.0, -1.0):
+        for f in (1.0, 0.999, 0.5, 2.0 ** -20):
+            t = s * bound * f
+            with np.errstate(all="ignore"):
+                ok = np.where(np.isfinite(c), c - t, c)
+            assert np.array_equal(ok[np.isfinite(c)], c[np.isfinite(c)])
