@@ -178,6 +178,9 @@ int kg_prepare(const kg_params* p, KgDev* d)
     d->u0 = p->gamma * (p->teq - 0.0);
     d->m0 = d->a_pi * kg_atan(d->u0);
     d->t_small = kg_absorb_bound(p->teq);
+    /* 1 - phi == 1 needs |phi| <= bound(1) = 2^-55, phi - 0.5 == -0.5 needs bound(0.5) = 2^-56 */
+    d->phi_small = kg_absorb_bound(0.5);
+    d->r0 = -0.5 + d->m0;
     return KG_OK;
 }
 

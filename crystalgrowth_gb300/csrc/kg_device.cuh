@@ -25,7 +25,13 @@
  *     gamma*Teq likewise; where |T| is small enough that Teq - T rounds to
  *     Teq (a bound from the host), the argument itself is not computed;
  *   - the Laplacians' 2 (E+W+N+S) + NE is one FMA: 2 x is exact, so the
- *     reference's two roundings are the FMA's one (kg_twice_plus).
+ *     reference's two roundings are the FMA's one (kg_twice_plus);
+ *   - where the E/W and N/S neighbours' eps^2 are equal (every cell whose
+ *     neighbourhood the front has not reached), grad eps^2 is +0 and the term
+ *     grad eps^2 . grad phi is a signed zero: its sign, and the sum it joins,
+ *     are settled on bit patterns;
+ *   - for |phi| <= 2^-56 the double well phi (1 - phi) (phi - 0.5 + m) is
+ *     exactly phi (m - 0.5): the other factors round to 1 and -0.5.
  * Comparisons use the bit patterns (integer pipe), never the FP64 pipe.
  */
 #pragma once
@@ -44,6 +50,8 @@ struct KgDev {
     double eps0, epsd0, e2_0, ee0; /* eps, eps', eps^2, eps eps' at arg0 */
     double u0, m0;    /* gamma (Teq - 0) and (alpha/pi) atan(u0) */
     uint64_t t_small; /* |T| bit patterns up to this leave Teq - T == Teq, so u == u0 */
+    uint64_t phi_small; /* |phi| bit patterns up to this leave 1 - phi == 1 and phi - 0.5 == -0.5 */
+    double r0;          /* -0.5 + m0: the double-well factor (phi - 0.5 + m) of such a cell */
 };
 
 #define KG_ABS_MASK 0x7fffffffffffffffull
@@ -150,6 +158,10 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
 #ifndef KG_FUSE
 #define KG_FUSE 1
 #endif
+/* 1: the flat-eps^2 and small-phi shortcuts of stage 2 (both exact); 0: the plain sequence */
+#ifndef KG_FAR
+#define KG_FAR 1
+#endif
 
 /* 9-point Laplacian in the reference's summation order (src/Kobayashi.cpp:142-151). */
 __device__ __forceinline__ double kg_lap(const KgDev& P, double c, double e, double w, double n, double s, double ne,
@@ -178,11 +190,33 @@ __device__ __forceinline__ void kg_stage2(const KgDev& P, double e2c, double gx,
                                           double lap_phi, double lap_t, double& phi, double& t,
                                           KgS2Aux* aux = nullptr)
 {
-    double gex = kg_idiv(e2E - e2W, &P.idx);
-    double gey = kg_idiv(e2N - e2S, &P.idy);
     double term1 = kg_idiv(aN - aS, &P.idy);
     double term2 = -kg_idiv(bE - bW, &P.idx);
-    double term3 = gex * gx + gey * gy;
+    /* the reference's sum term1 + term2 + e2c lap + term3 + reaction, left to right */
+    double acc = term1 + term2 + e2c * lap_phi;
+    double gex, gey;
+#if KG_FAR
+    const uint64_t ue = kg_bits(e2E), un = kg_bits(e2N);
+    if (ue == kg_bits(e2W) && un == kg_bits(e2S) && (ue & KG_ABS_MASK) < KG_INF_BITS &&
+        (un & KG_ABS_MASK) < KG_INF_BITS && (kg_bits(gx) & KG_ABS_MASK) < KG_INF_BITS &&
+        (kg_bits(gy) & KG_ABS_MASK) < KG_INF_BITS) {
+        /* e2E - e2W = +0 and e2N - e2S = +0, so gex = gey = +0 and term3 = (+0 gx) + (+0 gy): a zero
+         * that is -0 only when both products are, i.e. both gx and gy carry a sign bit.  Adding it
+         * leaves a nonzero acc unchanged; for a zero acc the sum is -0 only if both are -0. */
+        gex = 0.0;
+        gey = 0.0;
+        const uint64_t z3 = kg_bits(gx) & kg_bits(gy) & ~KG_ABS_MASK;
+        const uint64_t ua = kg_bits(acc);
+        if ((ua & KG_ABS_MASK) == 0)
+            acc = kg_from_bits(ua & z3);
+    } else
+#endif
+    {
+        gex = kg_idiv(e2E - e2W, &P.idx);
+        gey = kg_idiv(e2N - e2S, &P.idy);
+        double term3 = gex * gx + gey * gy;
+        acc = acc + term3;
+    }
     double m = P.m0;
 #if KG_FUSE
     if ((kg_bits(t) & KG_ABS_MASK) > P.t_small)
@@ -194,7 +228,14 @@ __device__ __forceinline__ void kg_stage2(const KgDev& P, double e2c, double gx,
     }
     double old_phi = phi;
     double old_t = t;
-    double rhs = term1 + term2 + e2c * lap_phi + term3 + old_phi * (1.0 - old_phi) * (old_phi - 0.5 + m);
+    double react;
+#if KG_FAR
+    if ((kg_bits(old_phi) & KG_ABS_MASK) <= P.phi_small)
+        react = old_phi * (kg_bits(m) == kg_bits(P.m0) ? P.r0 : -0.5 + m);
+    else
+#endif
+        react = old_phi * (1.0 - old_phi) * (old_phi - 0.5 + m);
+    double rhs = acc + react;
     double new_phi = old_phi + kg_idiv(rhs * P.dt, &P.itau);
     t = old_t + lap_t * P.dt + P.K * (new_phi - old_phi);
     phi = new_phi;
