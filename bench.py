@@ -1,11 +1,14 @@
 """Benchmark of the fused Kobayashi step on GB300 (FP64 cell-updates/s).
 
-Workload (the spec throughput case): one 8192 x 8192 FP64 grid, 64
+Workload (the headline throughput case): one 8192 x 8192 FP64 grid, 64
 seeded disks of radius 4..8, reference parameters with delta = 0.02 and
-theta0 = 0.2; the state advances in CUDA-graph chunks of 100 explicit steps.
-One bench step = one chunk = 100 time steps = 6.71e9 cell-updates.  The
-state is 3.2 GB (two copies of phi, T, theta), far above the 129 MB L2, so no
-flush is needed between timed chunks.
+theta0 = 0.2, 10,000 explicit steps advanced in CUDA-graph chunks of 100.
+One bench step = one chunk = 100 time steps = 6.71e9 cell-updates.  After W
+warm-up chunks the state is re-seeded, and K chunks are timed from step 0:
+the default K = 100 is the whole 10,000-step trajectory, over which the
+crystals (and the costlier interface cells) grow.  The state is 3.2 GB (two
+copies of phi, T, theta), far above the 129 MB L2, so no flush is needed
+between timed chunks.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -316,35 +319,33 @@ def run_ours(args, rank, world):
     sim = Kobayashi(nx, ny, cfg["params"]["dt"], params=cfg["params"])
     sim.seed_disks(cfg["disks"])
     sim.set_graph_chunk(CHUNK)
+    if args.tile:
+        sim.set_tile(*(int(v) for v in args.tile.split(",")))
     stream = torch.cuda.ExternalStream(sim.stream())
 
-    if args.full_run:
-        # the whole trajectory from the initial state; one untimed chunk first builds the graph,
-        # then the state is re-seeded so the timed run starts at step 0
-        args.warmup, args.steps = 1, cfg["steps"] // CHUNK
+    # warm-up chunks (graph build, clocks), then the state is re-seeded: the timed chunks are time
+    # steps 0 .. 100 K of the workload's trajectory (K = 100: the whole 10,000-step run)
+    for _ in range(args.warmup):
         sim.step(CHUNK)
-        sim.seed_disks(cfg["disks"])
-    else:
-        # warm-up chunks (the trajectory continues from here)
-        for _ in range(args.warmup):
-            sim.step(CHUNK)
+    sim.seed_disks(cfg["disks"])
     sim.sync()
 
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
+    # one event at every chunk boundary: the whole timed run, and the time of each 100-step chunk
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     clocks = Clocks(local)
     clocks.start()
     barrier(world)
     torch.cuda.synchronize()
-    ev0.record(stream)
-    for _ in range(args.steps):
+    evs[0].record(stream)
+    for k in range(args.steps):
         sim.step(CHUNK)
-    ev1.record(stream)
-    ev1.synchronize()
+        evs[k + 1].record(stream)
+    evs[-1].synchronize()
     torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
+    ms = evs[0].elapsed_time(evs[-1])
+    chunk_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
     ms = max_over_ranks(ms, world)
     ms_per_step = ms / args.steps
     value = world * cells * CHUNK * args.steps / (ms / 1e3)
@@ -370,14 +371,23 @@ def run_ours(args, rank, world):
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_CELL * cells / launch_s / 1e9
     traffic, prof = profile_traffic()
+    # the FP64 pipe's share at the time steps whose FP64 operation count ncu measured (per cell, on
+    # 4096^2 with the same disk density and strip shape): that step's chunk time, from the events
     fp64 = None
-    ops = prof.get("fp64_thread_ops_per_launch_8192") if nx == 8192 and ny == 8192 else None
-    if ops:
-        pk = fp64_peak()
-        fp64 = {"bound": "fp64 pipe", "achieved": ops / launch_s / 1e9, "peak": pk / 1e9, "unit": "GFLOP-ops/s",
-                "frac": ops / launch_s / pk, "ops_per_cell_update": ops / cells,
-                "peak_kind": "measured now (kg_diag_fp64_peak, DFMA lanes/s)",
-                "ops_source": "ncu DADD+DMUL+DFMA thread instructions of one mid-window launch "
+    samples = prof.get("fp64_ops_per_cell_at_step", {}) if nx == 8192 and ny == 8192 else {}
+    pts = []
+    pk = None
+    for step, opc in sorted((int(k), float(v)) for k, v in samples.items()):
+        k = step // CHUNK
+        if k < len(chunk_ms):
+            pk = pk or fp64_peak()
+            t = chunk_ms[k] / 1e3 / CHUNK
+            pts.append({"step": step, "ops_per_cell_update": opc, "achieved": opc * cells / t / 1e9,
+                        "frac": opc * cells / t / pk})
+    if pts:
+        fp64 = {"bound": "fp64 pipe", "unit": "GFLOP-ops/s", "peak": pk / 1e9,
+                "peak_kind": "measured now (kg_diag_fp64_peak, DFMA lanes/s)", "at_steps": pts,
+                "ops_source": "ncu DADD+DMUL+DFMA thread instructions per cell at those steps "
                               "(profiles/kg_step_kernel_traffic.json)"}
     line = {"metric": "fp64_cell_updates_per_s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -385,9 +395,10 @@ def run_ours(args, rank, world):
             "config": {"workload": "grid_%d: %dx%d FP64 Kobayashi step, %d seeded disks r=4..8, "
                                    "delta=0.02 theta0=0.2" % (nx, nx, ny, args.disks),
                        "bench_step": "one CUDA graph of %d time steps" % CHUNK,
-                       "steps_timed": ("the full trajectory, time steps 0..%d" % (args.steps * CHUNK)) if args.full_run
-                       else "time steps %d..%d of the trajectory" % (args.warmup * CHUNK,
-                                                                     (args.warmup + args.steps) * CHUNK),
+                       "steps_timed": "time steps 0..%d of the trajectory from the seeded state (the "
+                                      "workload is 10,000 steps)" % (args.steps * CHUNK),
+                       "e2e_steps": "%d chunks continuing from the timed run's final state" % e2e_steps,
+                       "strips": "%d threads x %d rows" % sim.tile(),
                        "l2": "inputs larger than L2 (3.2 GB state)", "parallelism": "replicas" if world > 1 else "1 GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
@@ -396,6 +407,7 @@ def run_ours(args, rank, world):
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": 3 * 8 * cells,
                     "d2h_bytes_per_step": 3 * 8 * cells},
             "gpu_launches": args.steps * CHUNK,
+            "chunk_ms": {"first": chunk_ms[0], "median": statistics.median(chunk_ms), "last": chunk_ms[-1]},
             "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(cfg)
@@ -411,16 +423,15 @@ def run_ours(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100,
+                    help="chunks of 100 time steps to time, from the seeded state (100: the whole 10,000-step run)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the ensemble and adjoint side measurements")
     ap.add_argument("--grid", type=int, default=8192, help="side of the square grid (8192 = the benchmark workload)")
-    ap.add_argument("--full-run", action="store_true",
-                    help="time the whole 10,000-step trajectory of the 8192^2 workload instead of a window "
-                         "(--steps/--warmup are ignored; about two minutes on one GB300)")
     ap.add_argument("--disks", type=int, default=64)
+    ap.add_argument("--tile", default="", help="strip shape NT,BH (default: the library's choice for the grid)")
     args = ap.parse_args()
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":

@@ -122,7 +122,60 @@ def main():
     pio2_hi, pio2_lo = hilo(pio2)
     out.append(f"#define KG_PIO2_HI {fmt(pio2_hi)}")
     out.append(f"#define KG_PI {fmt(rn(mp.pi))}")
+    out += fixed_point_tables()
     print("\n".join(out))
+
+
+def q(x, bits):
+    """x * 2^bits rounded to the nearest integer (exact rational arithmetic)."""
+    v = exact(x) * (Fraction(2) ** bits)
+    return int(v + Fraction(1, 2)) if v >= 0 else -int(-v + Fraction(1, 2))
+
+
+def u64(v):
+    """a 64-bit literal for a value in [-2^63, 2^64) (negative values in two's complement)"""
+    assert -(1 << 63) <= v < (1 << 64)
+    return "0x%016xull" % (v & ((1 << 64) - 1))
+
+
+def fixed_point_tables():
+    """Tables of the integer-pipe atan and sin/cos (fixed point, Qn = value * 2^n).
+
+    atan: for the node c_k = k/128 (k = 0..128), atan(c_k) in Q64 and the
+    Taylor coefficients a_1..a_7 of atan around c_k in Q62 (signed).
+    sin/cos: sin(n pi/128), cos(n pi/128) for n = 0..255 in Q62 (signed).
+    Reduction: 128/pi in Q122 as two 64-bit words, pi/128 in Q68, pi/2 in Q62.
+    Polynomials: atan(t)/t - 1 = -z (1/3 - z (1/5 - z (1/7 - z/9))), z = t^2,
+    coefficients in Q64; sin(r)/r - 1 = z H(z), 1 - cos(r) = z G(z), z = r^2,
+    H, G coefficients in Q63 (signed)."""
+    out = []
+    out.append("/* integer-pipe atan, entry k (8 words): atan(k/128) Q64, a1..a7 Q62 (signed) */")
+    out.append("#define KG_ATANX_TAB_DATA { \\")
+    for k in range(ATAN_N + 1):
+        a = atan_taylor(k, ATAN_N, ATAN_DEG)
+        row = [q(mp.atan(mp.mpf(k) / ATAN_N), 64)] + [q(a[n], 62) for n in range(1, ATAN_DEG + 1)]
+        assert row[0] < (1 << 64) and all(-(1 << 63) <= v < (1 << 63) for v in row[1:])
+        out.append("  " + ", ".join(u64(v) for v in row) + ", \\")
+    out.append("}")
+    out.append("/* integer-pipe sin/cos, entry n: sin(n pi/128), cos(n pi/128) in Q62 (signed) */")
+    out.append("#define KG_SCX_TAB_DATA { \\")
+    h = mp.pi / 128
+    for n in range(SC_N):
+        out.append("  " + u64(q(mp.sin(n * h), 62)) + ", " + u64(q(mp.cos(n * h), 62)) + ", \\")
+    out.append("}")
+    k = q(128 / mp.pi, 122)
+    assert k < (1 << 128)
+    out.append("#define KG_X_INVH_HI %s /* 128/pi in Q122, high word */" % u64(k >> 64))
+    out.append("#define KG_X_INVH_LO %s /* low word */" % u64(k & ((1 << 64) - 1)))
+    out.append("#define KG_X_H68 %s /* pi/128 in Q68 */" % u64(q(h, 68)))
+    out.append("#define KG_X_PIO2_62 %s /* pi/2 in Q62 */" % u64(q(mp.pi / 2, 62)))
+    for n in (3, 5, 7, 9):
+        out.append("#define KG_X_ATAN_I%d %s /* 1/%d in Q64 */" % (n, u64(q(mp.mpf(1) / n, 64)), n))
+    for name, v in (("H0", mp.mpf(-1) / 6), ("H1", mp.mpf(1) / 120), ("H2", mp.mpf(-1) / 5040),
+                    ("H3", mp.mpf(1) / 362880), ("G0", mp.mpf(1) / 2), ("G1", mp.mpf(-1) / 24),
+                    ("G2", mp.mpf(1) / 720), ("G3", mp.mpf(-1) / 40320)):
+        out.append("#define KG_X_%s ((int64_t)%s) /* %s in Q63 */" % (name, u64(q(v, 63)), mp.nstr(v, 8)))
+    return out
 
 
 if __name__ == "__main__":

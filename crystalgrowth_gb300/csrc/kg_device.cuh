@@ -17,7 +17,8 @@
  * FP64 (this file is compiled with -fmad=false, so a*b+c is never fused
  * unless written as kg_fma), with three exact shortcuts:
  *   - divisions by dx, dy, 3 dx^2 and tau use kg_idiv: the IEEE quotient's
- *     bits from 64-bit integer arithmetic, off the FP64 pipe;
+ *     bits from 64-bit integer arithmetic, off the FP64 pipe; the angle's
+ *     gy/gx uses kg_gdiv, the same for a divisor that varies per cell;
  *   - eps, eps' for the angle value theta = 0 (every cell the front has not
  *     reached) come from a table computed once on the host with the same
  *     kg_sincos, keyed on the exact bits of the sine/cosine argument;
@@ -68,6 +69,12 @@ __device__ __forceinline__ bool kg_neg_big(uint64_t b)
     return b > (0x8000000000000000ull | KG_EPS_BITS) && b <= 0xfff0000000000000ull;
 }
 
+/* 1: the angle's quotient gy/gx through kg_gdiv (the IEEE bits on the integer pipes); 0: the
+ * hardware division */
+#ifndef KG_GDIV
+#define KG_GDIV 1
+#endif
+
 /* Stage-1 quantities of one cell that its neighbours read in stage 2. */
 struct KgS1 {
     double gx, gy, e2, a, b; /* phi_x, phi_y, eps^2, eps eps' phi_x, eps eps' phi_y */
@@ -112,7 +119,11 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
     }
     bool use_atan = gx_neg || (gx_pos && (gy_pos || gy_neg));
     if (use_atan) {
+#if KG_GDIV
+        double at = kg_atan(kg_gdiv(gy, gx));
+#else
         double at = kg_atan(gy / gx);
+#endif
         double s = (gx_neg ? KG_PI : 2.0 * KG_PI) + at;
         theta = (gx_neg || gy_neg) ? s : at;
     }

@@ -35,6 +35,10 @@ __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double
             r = kg_twice_plus(v, x[n - 1 - i]);
         } else if (fn == KG_FN_MUL2_ADD) {
             r = __dadd_rn(__dmul_rn(2.0, v), x[n - 1 - i]);
+        } else if (fn == KG_FN_GDIV) {
+            r = kg_gdiv(v, x[n - 1 - i]);
+        } else if (fn == KG_FN_DIV_PAIR) {
+            r = v / x[n - 1 - i];
         }
         y[i] = r;
     }
@@ -42,7 +46,7 @@ __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double
 
 extern "C" int kg_diag_eval(int fn, const double* x, double* y, long long n, double b)
 {
-    if (fn < KG_FN_ATAN || fn > KG_FN_MUL2_ADD || n < 0 || (n > 0 && (!x || !y)))
+    if (fn < KG_FN_ATAN || fn > KG_FN_DIV_PAIR || fn == 12 || n < 0 || (n > 0 && (!x || !y)))
         return kg_fail(KG_ERR_INVALID, "kg_diag_eval: bad arguments");
     double yh = 0, yl = 0;
     kg_idivc ic;

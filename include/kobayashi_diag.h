@@ -25,6 +25,8 @@ extern "C" {
 #define KG_FN_MUL2 9  /* y = 2 x, the hardware multiplication */
 #define KG_FN_TWICE_PLUS 10 /* y[i] = kg_twice_plus(x[i], x[n-1-i]): 2 x + y in one FMA */
 #define KG_FN_MUL2_ADD 11   /* y[i] = 2 x[i] + x[n-1-i], two hardware roundings */
+#define KG_FN_GDIV 13       /* y[i] = kg_gdiv(x[i], x[n-1-i]): integer-pipe division, any divisor */
+#define KG_FN_DIV_PAIR 14   /* y[i] = x[i] / x[n-1-i], the GPU's own IEEE division */
 
 /* Evaluates function `fn` on n host values on the current device (synchronous). */
 KG_API int kg_diag_eval(int fn, const double* x, double* y, long long n, double b);

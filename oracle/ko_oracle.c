@@ -184,7 +184,8 @@ long long ko_kg_cdiv_check(const double* a, long long n, double b)
 
 /* host evaluation of kg_math.h over an array: fn 0 atan, 1 sin, 2 cos, 3 kg_cdiv(x, b), 4 x / b,
  * 5 kg_idiv(x, b), 6 kg_iadd(x[i], x[n-1-i]), 7 x[i] + x[n-1-i], 8 kg_imul2(x), 9 2 x,
- * 10 kg_twice_plus(x[i], x[n-1-i]), 11 2 x[i] + x[n-1-i] (two roundings), 12 kg_absorb_bound(x) */
+ * 10 kg_twice_plus(x[i], x[n-1-i]), 11 2 x[i] + x[n-1-i] (two roundings), 12 kg_absorb_bound(x),
+ * 13 kg_gdiv(x[i], x[n-1-i]), 14 x[i] / x[n-1-i], 15 kg_atan_f64(x) */
 int ko_kg_eval(int fn, const double* x, double* y, long long n, double b)
 {
     double yh = 0, yl = 0;
@@ -207,6 +208,9 @@ int ko_kg_eval(int fn, const double* x, double* y, long long n, double b)
         case 10: y[i] = kg_twice_plus(x[i], x[n - 1 - i]); break;
         case 11: y[i] = 2.0 * x[i] + x[n - 1 - i]; break;
         case 12: y[i] = kg_from_bits(kg_absorb_bound(x[i])); break;
+        case 13: y[i] = kg_gdiv(x[i], x[n - 1 - i]); break;
+        case 14: y[i] = x[i] / x[n - 1 - i]; break;
+        case 15: y[i] = kg_atan_f64(x[i]); break;
         default: return -1;
         }
     }

@@ -20,7 +20,8 @@ shipped), on small cases, and stores what it produced:
                             kg_math and the C library after 2000 steps
 
 Needs the reference checkout (only present where fixtures are made).
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [--only-kgm]
+(--only-kgm rewrites kgm_grid300.json alone, after a change to kg_math.h)
 """
 import hashlib
 import json
@@ -63,6 +64,10 @@ def run_ref(nx, ny, params, steps, fp64=True, init=None, via_update=False):
 
 def main():
     ko_oracle.build()
+    only_kgm = "--only-kgm" in sys.argv[1:]
+    if only_kgm:
+        write_kgm()
+        return
     # 1, 2: reference defaults on 64x48 through iUpdate
     for fp64, name in ((True, "ref64_default_64x48.npz"), (False, "ref32_default_64x48.npz")):
         r = run_ref(64, 48, DEFAULT, 200, fp64=fp64, via_update=True)
@@ -97,7 +102,16 @@ def main():
                max_phi=float(phi.max()), max_T=float(np.abs(t).max()), sum_phi=float(phi.sum()))
     with open(os.path.join(HERE, "ref64_grid300.json"), "w") as f:
         json.dump(ref, f, indent=1)
-    # 6: the same through kg_math (what the GPU computes), theta0 = 0 and 0.2
+    write_kgm()
+    print("fixtures written to", HERE)
+
+
+def write_kgm():
+    """6: the 300^2 case through kg_math (what the GPU computes), theta0 = 0 and 0.2, with the noise
+    floor against the C library's functions"""
+    cfg = configs.grid_300()
+    p0 = dict(cfg["params"], theta0=0.0)
+    init = configs.initial_fields(300, 300, cfg["disks"])
     out = dict(steps=cfg["steps"], disks=cfg["disks"])
     for tag, prm in (("theta0_0", p0), ("theta0_02", cfg["params"])):
         a = ko_oracle.port_run(*init, prm, cfg["steps"], libm=False, threads=8)
@@ -107,7 +121,6 @@ def main():
                         noise_floor_T=float(np.abs(a[1] - b[1]).max() / np.abs(b[1]).max()))
     with open(os.path.join(HERE, "kgm_grid300.json"), "w") as f:
         json.dump(out, f, indent=1)
-    print("fixtures written to", HERE)
 
 
 if __name__ == "__main__":

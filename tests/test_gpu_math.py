@@ -95,3 +95,23 @@ def test_twice_plus_equals_two_roundings_on_device():
         with np.errstate(all="ignore"):
             a, r = dev_eval(10, x), dev_eval(11, x)
             assert (((a.view(np.uint64) == r.view(np.uint64)) | (np.isnan(a) & np.isnan(r))).all())
+
+
+def test_gdiv_equals_ieee_division_on_device():
+    """kg_gdiv(x[i], x[n-1-i]) on the device has the bits of the GPU's own IEEE division"""
+    rng = np.random.default_rng(79)
+    n = 2_000_000
+    a = rng.standard_normal(n) * 10.0 ** rng.integers(-300, 300, n)
+    near = np.concatenate([1 + rng.integers(0, 2 ** 20, n) * 2.0 ** -52, 2 - rng.integers(1, 2 ** 20, n) * 2.0 ** -52])
+    m = rng.uniform(1, 2, n)
+    edge = np.array([0.0, -0.0, 1.0, -1.0, 3.0, 2.0 ** -1022, 5e-324, -5e-324, 1.7976931348623157e308,
+                     2.0 ** 1000, 2.0 ** -1000, math.inf, -math.inf, math.nan, 0.1, 1e-300, 1e300, 7.0])
+    cases = [np.concatenate([a, a[::-1] * rng.uniform(0.5, 2, n)]), near * rng.choice([-1, 1], 2 * n),
+             np.concatenate([m, m[::-1]]),
+             np.concatenate([rng.uniform(1, 2, n) * 2.0 ** 1000, rng.uniform(1, 2, n) * 2.0 ** -30]),
+             np.concatenate([rng.uniform(1, 2, n) * 2.0 ** -1000, rng.uniform(1, 2, n) * 2.0 ** 30]),
+             np.concatenate([edge, np.resize(edge[::-1], edge.size)])]
+    for x in cases:
+        with np.errstate(all="ignore"):
+            a_, r_ = dev_eval(13, x), dev_eval(14, x)
+            assert (((a_.view(np.uint64) == r_.view(np.uint64)) | (np.isnan(a_) & np.isnan(r_))).all())
