@@ -164,9 +164,30 @@ def cpu_baseline_sample(cfg, seconds_budget=20.0):
         step(extra)
         per = (time.perf_counter() - t2) / extra
         n_steps += extra
-    return {"value": nx * ny / per, "unit": "cell-updates/s", "cores": 1, "kind": kind,
-            "sample": "%d time step(s) of the %dx%d FP64 state, single thread (the reference is single-threaded)"
-                      % (n_steps, nx, ny)}
+    out = {"value": nx * ny / per, "unit": "cell-updates/s", "cores": 1, "kind": kind,
+           "sample": "%d time step(s) of the %dx%d FP64 state, single thread (the reference is single-threaded)"
+                     % (n_steps, nx, ny)}
+    # beside it: the reference as shipped (FP32, single thread), and the C restatement (FP64, C library
+    # math) with OpenMP over all host cores -- two time steps each of the same state
+    try:
+        r32 = ko_oracle.Reference(nx, ny, p["dt"], fp64=False)
+        r32.set_params(p)
+        r32.set_state(*init)
+        r32.step(1)
+        t0 = time.perf_counter()
+        r32.step(2)
+        out["fp32_as_shipped"] = {"value": 2 * nx * ny / (time.perf_counter() - t0), "cores": 1,
+                                  "kind": "reference", "sample": "2 time steps, FP32 build as shipped"}
+        del r32
+    except (FileNotFoundError, OSError):
+        pass
+    cores = os.cpu_count() or 1
+    st = ko_oracle.port_run(*init, p, 1, libm=True, threads=cores)
+    t0 = time.perf_counter()
+    ko_oracle.port_run(*st, p, 2, libm=True, threads=cores)
+    out["restatement_all_cores"] = {"value": 2 * nx * ny / (time.perf_counter() - t0), "cores": cores,
+                                    "kind": "port", "sample": "2 time steps, FP64, OpenMP over rows"}
+    return out
 
 
 def measure_ensemble(steps=100, trial_steps=10):
@@ -352,21 +373,23 @@ def run_ours(args, rank, world):
     launch_s = ms_per_step / 1e3 / CHUNK  # average duration of one step-kernel launch
 
     # end to end through the C ABI with host buffers: upload state, 100 steps, download state
-    pinned = [torch.empty((ny, nx), dtype=torch.float64, pin_memory=True) for _ in range(3)]
-    host = [t.numpy() for t in pinned]
-    for h, v in zip(host, sim.fields()):
-        h[...] = v
-    e2e_steps = max(1, min(args.steps, 3))
-    barrier(world)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        sim.set_fields(*host)
-        sim.step(CHUNK)
-        sim.fields(out=host)
-    t1 = time.perf_counter()
-    e2e_s = max_over_ranks(t1 - t0, world)
-    e2e_value = world * cells * CHUNK * e2e_steps / e2e_s
+    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 3))
+    e2e_value = None
+    if e2e_steps:
+        pinned = [torch.empty((ny, nx), dtype=torch.float64, pin_memory=True) for _ in range(3)]
+        host = [t.numpy() for t in pinned]
+        for h, v in zip(host, sim.fields()):
+            h[...] = v
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            sim.set_fields(*host)
+            sim.step(CHUNK)
+            sim.fields(out=host)
+        t1 = time.perf_counter()
+        e2e_s = max_over_ranks(t1 - t0, world)
+        e2e_value = world * cells * CHUNK * e2e_steps / e2e_s
 
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_CELL * cells / launch_s / 1e9
@@ -432,6 +455,7 @@ def main():
     ap.add_argument("--grid", type=int, default=8192, help="side of the square grid (8192 = the benchmark workload)")
     ap.add_argument("--disks", type=int, default=64)
     ap.add_argument("--tile", default="", help="strip shape NT,BH (default: the library's choice for the grid)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (short profiling runs)")
     args = ap.parse_args()
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":

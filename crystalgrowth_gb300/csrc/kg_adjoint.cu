@@ -37,6 +37,8 @@
 
 struct KgAdj {
     double inv_dx, inv_dy, inv_lap, dt, dt_tau, tau, K, eb, delta, j, a_pi, gamma, teq, u0, inv0;
+    /* products of parameters the reverse passes use per cell */
+    double inv_tau, eb_delta, k_e, k_d, k_j, a_pi_gamma, a_pi_teq;
 };
 
 template <int NT>
@@ -94,54 +96,58 @@ __global__ void __launch_bounds__(KG_ADJ_THREADS) kg_adj_pass_ab(const __grid_co
         int ip = i + 1 == nx ? 0 : i + 1, im = i == 0 ? nx - 1 : i - 1;
         int jp = j + 1 == ny ? 0 : j + 1, jm = j == 0 ? ny - 1 : j - 1;
         long long cE = kg_nb(ip, j, nx), cW = kg_nb(im, j, nx), cN = kg_nb(i, jp, nx), cS = kg_nb(i, jm, nx);
-        /* pass A at c */
+        /* pass A at c (explicit FMAs: the adjoint is checked to a tolerance, not bit for bit) */
         double phi = tp.f[KG_TAPE_PHI][c], t = tp.f[KG_TAPE_T][c];
         double lap = tp.f[KG_TAPE_LAP][c], R = tp.f[KG_TAPE_RHS][c], m = tp.f[KG_TAPE_M][c];
         double s = tp.f[KG_TAPE_SIN][c], co = tp.f[KG_TAPE_COS][c];
-        double eps = A.eb * (1.0 + A.delta * co);
+        double eps = kg_fma(A.eb_delta, co, A.eb);
         double lp = lphi1[c], lt = lt1[c];
-        double lRc = (lp + A.K * lt) * A.dt_tau;
-        double q = phi - 0.5 + m;
-        double pp = phi * (1.0 - phi);
-        double dw = (1.0 - 2.0 * phi) * q + pp;
+        double lRc = kg_fma(A.K, lt, lp) * A.dt_tau;
+        double q = (phi - 0.5) + m;
+        double pp = kg_fma(-phi, phi, phi);                  /* phi (1 - phi) */
+        double dw = kg_fma(kg_fma(-2.0, phi, 1.0), q, pp);   /* (1 - 2 phi) q + phi (1 - phi) */
         double lm = lRc * pp;
         double u = A.gamma * (A.teq - t);
-        double inv = (u == A.u0) ? A.inv0 : 1.0 / (1.0 + u * u);
-        w.lLphi[c] = lRc * eps * eps;
+        double inv = (u == A.u0) ? A.inv0 : kg_gdiv(1.0, kg_fma(u, u, 1.0));
+        double lmi = lm * inv;
+        w.lLphi[c] = lRc * (eps * eps);
         w.lLT[c] = lt * A.dt;
-        w.lphi_loc[c] = lp + lRc * dw;
-        w.lT_loc[c] = lt - lm * A.a_pi * A.gamma * inv;
-        g[1] += lt * (phi_next[c] - phi);
-        g[3] += -lRc * R / A.tau;
-        g[4] += lm * A.a_pi * (A.teq - t) * inv;
+        w.lphi_loc[c] = kg_fma(lRc, dw, lp);
+        w.lT_loc[c] = kg_fma(-lmi, A.a_pi_gamma, lt);
+        g[1] = kg_fma(lt, phi_next[c] - phi, g[1]);
+        g[3] = kg_fma(-lRc, R * A.inv_tau, g[3]);
+        g[4] = kg_fma(lmi, kg_fma(-A.a_pi, t, A.a_pi_teq), g[4]);
         /* pass B at c, with the neighbours' lR recomputed */
-        double lRE = (lphi1[cE] + A.K * lt1[cE]) * A.dt_tau, lRW = (lphi1[cW] + A.K * lt1[cW]) * A.dt_tau;
-        double lRN = (lphi1[cN] + A.K * lt1[cN]) * A.dt_tau, lRS = (lphi1[cS] + A.K * lt1[cS]) * A.dt_tau;
+        double lRE = kg_fma(A.K, lt1[cE], lphi1[cE]) * A.dt_tau, lRW = kg_fma(A.K, lt1[cW], lphi1[cW]) * A.dt_tau;
+        double lRN = kg_fma(A.K, lt1[cN], lphi1[cN]) * A.dt_tau, lRS = kg_fma(A.K, lt1[cS], lphi1[cS]) * A.dt_tau;
         const double* GX = tp.f[KG_TAPE_GX];
         const double* GY = tp.f[KG_TAPE_GY];
         double gx = GX[c], gy = GY[c];
-        double le2 = lRc * lap + (lRW * GX[cW] - lRE * GX[cE]) * A.inv_dx + (lRS * GY[cS] - lRN * GY[cN]) * A.inv_dy;
+        double dxx = kg_fma(lRW, GX[cW], -(lRE * GX[cE]));
+        double dyy = kg_fma(lRS, GY[cS], -(lRN * GY[cN]));
+        double le2 = kg_fma(dxx, A.inv_dx, kg_fma(dyy, A.inv_dy, lRc * lap));
         double la = (lRS - lRN) * A.inv_dy;
         double lb = (lRE - lRW) * A.inv_dx;
-        double epsd = -A.eb * A.j * A.delta * s;
+        double epsd = A.k_d * s;
         double ee = eps * epsd;
-        double lq = la * gx + lb * gy;
-        double leps = 2.0 * eps * le2 + epsd * lq;
+        double lq = kg_fma(la, gx, lb * gy);
+        double leps = kg_fma(eps + eps, le2, epsd * lq);
         double lepsd = eps * lq;
-        double lgx = lRc * tp.f[KG_TAPE_GEX][c] + la * ee;
-        double lgy = lRc * tp.f[KG_TAPE_GEY][c] + lb * ee;
-        double lpsi = leps * (-A.eb * A.delta * s) + lepsd * (-A.eb * A.j * A.delta * co);
-        g[0] += leps * A.eb * co + lepsd * (-A.eb * A.j * s);
-        g[2] += -A.j * lpsi;
-        double lthp = lth1[c] + A.j * lpsi;
+        double lgx = kg_fma(lRc, tp.f[KG_TAPE_GEX][c], la * ee);
+        double lgy = kg_fma(lRc, tp.f[KG_TAPE_GEY][c], lb * ee);
+        double lpsi = kg_fma(leps, A.k_e * s, lepsd * (A.k_d * co));
+        g[0] = kg_fma(leps, A.eb * co, kg_fma(lepsd, A.k_j * s, g[0]));
+        g[2] = kg_fma(-A.j, lpsi, g[2]);
+        double lthp = kg_fma(A.j, lpsi, lth1[c]);
         uint64_t bx = kg_bits(gx), by = kg_bits(gy);
         bool gx_small = kg_small(bx), gx_pos = kg_pos_big(bx), gx_neg = kg_neg_big(bx);
         bool gy_big = kg_pos_big(by) || kg_neg_big(by);
         double lth = 0.0;
         if (gx_neg || (gx_pos && gy_big)) {
-            double r2 = 1.0 / (gx * gx + gy * gy);
-            lgx += lthp * (-gy) * r2;
-            lgy += lthp * gx * r2;
+            /* d atan(gy/gx) = (gx dgy - gy dgx) / (gx^2 + gy^2) */
+            double tr = lthp * kg_gdiv(1.0, kg_fma(gx, gx, gy * gy));
+            lgx = kg_fma(-gy, tr, lgx);
+            lgy = kg_fma(gx, tr, lgy);
         } else if (!(gx_small && gy_big)) {
             lth = lthp;
         }
@@ -163,13 +169,17 @@ __global__ void __launch_bounds__(KG_ADJ_THREADS) kg_adj_pass_c(const __grid_con
         int jp = j + 1 == ny ? 0 : j + 1, jm = j == 0 ? ny - 1 : j - 1;
         long long cE = kg_nb(ip, j, nx), cW = kg_nb(im, j, nx), cN = kg_nb(i, jp, nx), cS = kg_nb(i, jm, nx);
         long long cNE = kg_nb(ip, jp, nx), cNW = kg_nb(im, jp, nx), cSE = kg_nb(ip, jm, nx), cSW = kg_nb(im, jm, nx);
-        double sp = 2.0 * (w.lLphi[cE] + w.lLphi[cW] + w.lLphi[cN] + w.lLphi[cS]) + w.lLphi[cNE] + w.lLphi[cNW] +
-                    w.lLphi[cSE] + w.lLphi[cSW] - 12.0 * w.lLphi[c];
-        double st = 2.0 * (w.lLT[cE] + w.lLT[cW] + w.lLT[cN] + w.lLT[cS]) + w.lLT[cNE] + w.lLT[cNW] + w.lLT[cSE] +
-                    w.lLT[cSW] - 12.0 * w.lLT[c];
-        lphi0[c] = w.lphi_loc[c] + (w.lgx[cW] - w.lgx[cE]) * A.inv_dx + (w.lgy[cS] - w.lgy[cN]) * A.inv_dy +
-                   sp * A.inv_lap;
-        lt0[c] = w.lT_loc[c] + st * A.inv_lap;
+        /* the transposed 9-point Laplacians (the stencil is symmetric), with explicit FMAs */
+        double sp = kg_fma(2.0, (w.lLphi[cE] + w.lLphi[cW]) + (w.lLphi[cN] + w.lLphi[cS]),
+                           (w.lLphi[cNE] + w.lLphi[cNW]) + (w.lLphi[cSE] + w.lLphi[cSW]));
+        sp = kg_fma(-12.0, w.lLphi[c], sp);
+        double st = kg_fma(2.0, (w.lLT[cE] + w.lLT[cW]) + (w.lLT[cN] + w.lLT[cS]),
+                           (w.lLT[cNE] + w.lLT[cNW]) + (w.lLT[cSE] + w.lLT[cSW]));
+        st = kg_fma(-12.0, w.lLT[c], st);
+        double v = kg_fma(w.lgx[cW] - w.lgx[cE], A.inv_dx, w.lphi_loc[c]);
+        v = kg_fma(w.lgy[cS] - w.lgy[cN], A.inv_dy, v);
+        lphi0[c] = kg_fma(sp, A.inv_lap, v);
+        lt0[c] = kg_fma(st, A.inv_lap, w.lT_loc[c]);
     }
 }
 
@@ -242,6 +252,13 @@ static int adj_prepare(kg_adjoint* a, const kg_params* p)
     A.teq = p->teq;
     A.u0 = p->gamma * (p->teq - 0.0);
     A.inv0 = 1.0 / (1.0 + A.u0 * A.u0);
+    A.inv_tau = 1.0 / p->tau;
+    A.eb_delta = p->eps_bar * p->delta;            /* eps = eb + eb delta cos(psi) */
+    A.k_e = -p->eps_bar * p->delta;                /* d eps / d psi = k_e sin(psi) */
+    A.k_d = -p->eps_bar * p->aniso * p->delta;     /* eps' = k_d sin(psi); d eps'/d psi = k_d cos(psi) */
+    A.k_j = -p->eps_bar * p->aniso;                /* d eps' / d delta = k_j sin(psi) */
+    A.a_pi_gamma = A.a_pi * p->gamma;
+    A.a_pi_teq = A.a_pi * p->teq;
     return KG_OK;
 }
 
