@@ -352,6 +352,15 @@ typedef struct kg_idivc {
     int pow2;    /* b is a power of two */
 } kg_idivc;
 
+KG_HD int kg_clz64(uint64_t x)
+{
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)x);
+#else
+    return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
 KG_HD uint64_t kg_umulhi64(uint64_t a, uint64_t b)
 {
 #if defined(__CUDA_ARCH__)
@@ -394,6 +403,21 @@ KG_HD int kg_idiv_prepare(double b, kg_idivc* c)
     return 0;
 }
 
+/*
+ * sign | RN(Q 2^(e-1075)) for a quotient whose exact significand is Q = q + rem/B
+ * (q in [2^52, 2^53), rem in [0, B)) and whose biased exponent e < 1: a
+ * subnormal result (or zero), rounded once from the exact quotient.
+ */
+KG_HD double kg_round_subnormal(uint64_t sign, uint64_t q, uint64_t rem, int e)
+{
+    int s = 1 - e;
+    if (s > 53)
+        return kg_from_bits(sign);
+    uint64_t low = q & ((1ull << s) - 1), half = 1ull << (s - 1), m = q >> s;
+    m += (uint64_t)((low > half) | ((low == half) & ((rem != 0) | (int)(m & 1))));
+    return kg_from_bits(sign | m);
+}
+
 KG_HD double kg_idiv(double a, const kg_idivc* c)
 {
     uint64_t ua = kg_bits(a);
@@ -401,13 +425,22 @@ KG_HD double kg_idiv(double a, const kg_idivc* c)
     int ea = (int)((ua >> 52) & 0x7ff);
     if ((ua & 0x7fffffffffffffffull) == 0)
         return a;
-    if (ea == 0 || ea == 0x7ff)
+    if (ea == 0x7ff)
         return a / c->b;
-    uint64_t A = (ua & 0x000fffffffffffffull) | 0x0010000000000000ull;
+    uint64_t A;
+    if (ea == 0) { /* subnormal dividend: normalise its significand */
+        int sh = kg_clz64(ua & 0x7fffffffffffffffull) - 11;
+        A = (ua & 0x7fffffffffffffffull) << sh;
+        ea = 1 - sh;
+    } else {
+        A = (ua & 0x000fffffffffffffull) | 0x0010000000000000ull;
+    }
     if (c->pow2) {
         int e = ea - c->eb + 1023;
         if (e >= 1 && e <= 2046)
             return kg_from_bits(sign | ((uint64_t)e << 52) | (A & 0x000fffffffffffffull));
+        if (e < 1)
+            return kg_round_subnormal(sign, A, 0, e);
     } else {
         int shift = A < c->B;
         uint64_t Ap = A << shift;
@@ -417,23 +450,16 @@ KG_HD double kg_idiv(double a, const kg_idivc* c)
             q += 1;
             rem -= c->B;
         }
-        q += (rem << 1) > c->B;
         int e = ea - c->eb + 1023 - shift;
         if (e >= 1 && e <= 2046)
-            return kg_from_bits(sign | (((uint64_t)(e - 1) << 52) + q));
+            return kg_from_bits(sign | (((uint64_t)(e - 1) << 52) + q + ((rem << 1) > c->B)));
+        if (e < 1)
+            return kg_round_subnormal(sign, q, rem, e);
     }
     return a / c->b;
 }
 
 
-KG_HD int kg_clz64(uint64_t x)
-{
-#if defined(__CUDA_ARCH__)
-    return __clzll((long long)x);
-#else
-    return x ? __builtin_clzll(x) : 64;
-#endif
-}
 
 /*
  * a + b (IEEE binary64, round to nearest even) in 64-bit integer arithmetic,
@@ -576,8 +602,10 @@ KG_HD uint64_t kg_recip116(uint64_t B)
  *     and read as signed) corrects q and gives the rounding bit.  A quotient
  *     of two 53-bit significands is never halfway between two doubles
  *     unless B is a power of two, which is an exponent shift here.
- * Zero dividends give a signed zero; subnormal or non-finite operands, a zero
- * divisor and quotients outside the normal range take the hardware division.
+ * Zero dividends give a signed zero; subnormal operands are normalised and
+ * subnormal quotients rounded once from the exact remainder; non-finite
+ * operands, a zero divisor and overflowing quotients take the hardware
+ * division.
  */
 KG_HD double kg_gdiv(double a, double b)
 {
@@ -585,18 +613,31 @@ KG_HD double kg_gdiv(double a, double b)
     uint64_t ua = kg_bits(a), ub = kg_bits(b);
     uint64_t sign = (ua ^ ub) & 0x8000000000000000ull;
     int ea = (int)((ua >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff);
-    if (eb == 0 || eb == 0x7ff || ea == 0x7ff)
+    if (eb == 0x7ff || ea == 0x7ff || (ub & 0x7fffffffffffffffull) == 0)
         return a / b;
-    if (ea == 0) {
-        if ((ua & 0x7fffffffffffffffull) == 0)
-            return kg_from_bits(sign);
-        return a / b;
+    if ((ua & 0x7fffffffffffffffull) == 0)
+        return kg_from_bits(sign);
+    uint64_t A, B;
+    if (ea == 0) { /* subnormal operands: normalise the significands */
+        int sh = kg_clz64(ua & 0x7fffffffffffffffull) - 11;
+        A = (ua & 0x7fffffffffffffffull) << sh;
+        ea = 1 - sh;
+    } else {
+        A = (ua & MANT) | HID;
     }
-    uint64_t A = (ua & MANT) | HID, B = (ub & MANT) | HID;
+    if (eb == 0) {
+        int sh = kg_clz64(ub & 0x7fffffffffffffffull) - 11;
+        B = (ub & 0x7fffffffffffffffull) << sh;
+        eb = 1 - sh;
+    } else {
+        B = (ub & MANT) | HID;
+    }
     if (B == HID) {
         int e = ea - eb + 1023;
         if (e >= 1 && e <= 2046)
             return kg_from_bits(sign | ((uint64_t)e << 52) | (A & MANT));
+        if (e < 1)
+            return kg_round_subnormal(sign, A, 0, e);
         return a / b;
     }
     uint64_t R = kg_recip116(B);
@@ -612,10 +653,11 @@ KG_HD double kg_gdiv(double a, double b)
         q += 1;
         r -= (int64_t)B;
     }
-    q += (uint64_t)r * 2 > B;
     int e = ea - eb + 1023 - shift;
     if (e >= 1 && e <= 2046)
-        return kg_from_bits(sign | (((uint64_t)(e - 1) << 52) + q));
+        return kg_from_bits(sign | (((uint64_t)(e - 1) << 52) + q + ((uint64_t)r * 2 > B)));
+    if (e < 1)
+        return kg_round_subnormal(sign, q, (uint64_t)r, e);
     return a / b;
 }
 

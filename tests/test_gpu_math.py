@@ -46,7 +46,10 @@ def test_transcendentals_device_equals_host(fn):
 
 @pytest.mark.parametrize("b", [0.03, 3 * 0.03 * 0.03, 3e-4, 2.1e-4, 3.99e-4, 1e-4, 9e-4, 7.0, 1 / 3, 0.5, 2.0 ** -99])
 def test_constant_division_equals_ieee_on_device(b):
-    x = inputs(int(b * 1e7) % 997)
+    rng = np.random.default_rng(int(b * 1e7) % 991)
+    k = rng.integers(1, 53, 500_000)
+    sub = ((rng.integers(0, 2 ** 62, k.size, dtype=np.int64) % (2 ** k)) | 1).astype(np.float64) * 5e-324
+    x = np.concatenate([inputs(int(b * 1e7) % 997), sub, -sub])
     ieee = dev_eval(4, x, b)
     assert same_bits(dev_eval(3, x, b), ieee)
     assert same_bits(dev_eval(5, x, b), ieee)
@@ -98,7 +101,8 @@ def test_twice_plus_equals_two_roundings_on_device():
 
 
 def test_gdiv_equals_ieee_division_on_device():
-    """kg_gdiv(x[i], x[n-1-i]) on the device has the bits of the GPU's own IEEE division"""
+    """kg_gdiv(x[i], x[n-1-i]) on the device has the bits of the GPU's own IEEE division, subnormal
+    operands and quotients included"""
     rng = np.random.default_rng(79)
     n = 2_000_000
     a = rng.standard_normal(n) * 10.0 ** rng.integers(-300, 300, n)
@@ -111,6 +115,10 @@ def test_gdiv_equals_ieee_division_on_device():
              np.concatenate([rng.uniform(1, 2, n) * 2.0 ** 1000, rng.uniform(1, 2, n) * 2.0 ** -30]),
              np.concatenate([rng.uniform(1, 2, n) * 2.0 ** -1000, rng.uniform(1, 2, n) * 2.0 ** 30]),
              np.concatenate([edge, np.resize(edge[::-1], edge.size)])]
+    k = rng.integers(1, 53, n)
+    sub = ((rng.integers(0, 2 ** 62, n, dtype=np.int64) % (2 ** k)) | 1).astype(np.float64) * 5e-324
+    cases += [np.concatenate([sub, rng.uniform(0.01, 100, n)]), np.concatenate([sub, sub[::-1]]),
+              np.concatenate([rng.uniform(1, 2, n) * 2.0 ** rng.integers(-1060, -1000, n), sub[::-1]])]
     for x in cases:
         with np.errstate(all="ignore"):
             a_, r_ = dev_eval(13, x), dev_eval(14, x)

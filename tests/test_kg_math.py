@@ -279,3 +279,37 @@ def test_gdiv_every_significand_pair_small_grid():
     x = np.concatenate([a, d[::-1]])
     with np.errstate(all="ignore"):
         assert _same(ko_oracle.kg_eval(13, x), ko_oracle.kg_eval(14, x))
+
+
+def _subnormals(rng, n):
+    """every subnormal magnitude scale: random significand bits below 2^k, k = 1..52, both signs"""
+    k = rng.integers(1, 53, n)
+    m = (rng.integers(0, 2 ** 62, n, dtype=np.int64) % (2 ** k)).astype(np.int64) | 1
+    return (m.astype(np.float64) * 5e-324) * rng.choice([-1, 1], n)
+
+
+@pytest.mark.parametrize("b", [0.03, 3 * 0.03 * 0.03, 3e-4, 2.1e-4, 7.0, 1 / 3, 0.5, 2.0 ** -99, 2.0 ** 99, 1e-4])
+def test_idiv_subnormal_dividends(b):
+    """subnormal dividends (normalised on the integer pipes) and subnormal quotients (rounded once from
+    the exact remainder) have the bits of the IEEE division"""
+    rng = np.random.default_rng(int(b * 1e7) % 977 + 3)
+    x = np.concatenate([_subnormals(rng, 1_000_000), rng.uniform(1, 2, 200_000) * 2.0 ** rng.integers(-1080, -1000, 200_000)])
+    with np.errstate(all="ignore"):
+        ref = x / b
+    assert _same(ko_oracle.kg_eval(5, x, b), ref)
+
+
+def test_gdiv_subnormal_operands_and_results():
+    """kg_gdiv with subnormal dividends, subnormal divisors, and quotients in the subnormal range
+    (every rounding position) has the bits of the IEEE division"""
+    rng = np.random.default_rng(35)
+    n = 1_000_000
+    sub = _subnormals(rng, n)
+    cases = [np.concatenate([sub, rng.uniform(0.01, 100, n)]),                       # subnormal / normal
+             np.concatenate([rng.uniform(1, 2, n) * 2.0 ** rng.integers(-1060, -1000, n), sub[::-1]]),   # / subnormal
+             np.concatenate([rng.uniform(1, 2, n) * 2.0 ** rng.integers(-1022, -960, n),
+                             rng.uniform(1, 2, n) * 2.0 ** rng.integers(1, 110, n)]),  # normal / normal -> subnormal
+             np.concatenate([sub, sub[::-1]])]
+    for x in cases:
+        with np.errstate(all="ignore"):
+            assert _same(ko_oracle.kg_eval(13, x), ko_oracle.kg_eval(14, x))
