@@ -375,6 +375,7 @@ def run_ours(args, rank, world):
     # end to end through the C ABI with host buffers: upload state, 100 steps, download state
     e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 3))
     e2e_value = None
+    e2e_parts = None
     if e2e_steps:
         pinned = [torch.empty((ny, nx), dtype=torch.float64, pin_memory=True) for _ in range(3)]
         host = [t.numpy() for t in pinned]
@@ -382,22 +383,37 @@ def run_ours(args, rank, world):
             h[...] = v
         barrier(world)
         torch.cuda.synchronize()
+        parts = [0.0, 0.0, 0.0]  # upload, steps, download (host clock; the steps' part ends at a sync)
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            ta = time.perf_counter()
             sim.set_fields(*host)
+            tb = time.perf_counter()
             sim.step(CHUNK)
+            sim.sync()
+            tc = time.perf_counter()
             sim.fields(out=host)
+            td = time.perf_counter()
+            parts[0] += tb - ta
+            parts[1] += tc - tb
+            parts[2] += td - tc
         t1 = time.perf_counter()
         e2e_s = max_over_ranks(t1 - t0, world)
         e2e_value = world * cells * CHUNK * e2e_steps / e2e_s
+        state_bytes = 3 * 8 * cells
+        e2e_parts = {"upload_ms": 1e3 * parts[0] / e2e_steps, "steps_ms": 1e3 * parts[1] / e2e_steps,
+                     "download_ms": 1e3 * parts[2] / e2e_steps,
+                     "upload_gbs": state_bytes * e2e_steps / parts[0] / 1e9,
+                     "download_gbs": state_bytes * e2e_steps / parts[2] / 1e9}
 
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_CELL * cells / launch_s / 1e9
     traffic, prof = profile_traffic()
-    # the FP64 pipe's share at the time steps whose FP64 operation count ncu measured (per cell, on
-    # 4096^2 with the same disk density and strip shape): that step's chunk time, from the events
+    # the FP64 pipe's share at the time steps whose FP64-pipe load ncu measured (per cell, on 4096^2
+    # with the same disk density and strip shape): lane-slots = warp instructions on the FP64 pipe x 32,
+    # against the full-warp DFMA lane rate measured now; the time is that step's chunk, from the events
     fp64 = None
-    samples = prof.get("fp64_ops_per_cell_at_step", {}) if nx == 8192 and ny == 8192 else {}
+    samples = prof.get("fp64_lane_slots_per_cell_at_step", {}) if nx == 8192 and ny == 8192 else {}
     pts = []
     pk = None
     for step, opc in sorted((int(k), float(v)) for k, v in samples.items()):
@@ -405,12 +421,19 @@ def run_ours(args, rank, world):
         if k < len(chunk_ms):
             pk = pk or fp64_peak()
             t = chunk_ms[k] / 1e3 / CHUNK
-            pts.append({"step": step, "ops_per_cell_update": opc, "achieved": opc * cells / t / 1e9,
+            pts.append({"step": step, "lane_slots_per_cell_update": opc, "achieved": opc * cells / t / 1e9,
                         "frac": opc * cells / t / pk})
     if pts:
-        fp64 = {"bound": "fp64 pipe", "unit": "GFLOP-ops/s", "peak": pk / 1e9,
-                "peak_kind": "measured now (kg_diag_fp64_peak, DFMA lanes/s)", "at_steps": pts,
-                "ops_source": "ncu DADD+DMUL+DFMA thread instructions per cell at those steps "
+        # the nominal rate, 2 FP64 lanes per clock per SM at the highest SM clock sampled under load
+        nominal = None
+        if clk.get("sm_max_mhz"):
+            nominal = 2 * torch.cuda.get_device_properties(local).multi_processor_count * clk["sm_max_mhz"] * 1e6
+            for q in pts:
+                q["frac_of_nominal"] = q["achieved"] * 1e9 / nominal
+        fp64 = {"bound": "fp64 pipe", "unit": "G lane-slots/s", "peak": pk / 1e9,
+                "peak_kind": "measured now (kg_diag_fp64_peak, full-warp DFMA lanes/s)",
+                "nominal": nominal / 1e9 if nominal else None, "at_steps": pts,
+                "ops_source": "ncu sm__inst_executed_pipe_fp64 x 32 per cell at those steps "
                               "(profiles/kg_step_kernel_traffic.json)"}
     line = {"metric": "fp64_cell_updates_per_s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -428,7 +451,7 @@ def run_ours(args, rank, world):
                          "note": "48 B/cell algorithmic; the kernel is FP64-pipe bound on GB300"},
             "fp64_roofline": fp64,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": 3 * 8 * cells,
-                    "d2h_bytes_per_step": 3 * 8 * cells},
+                    "d2h_bytes_per_step": 3 * 8 * cells, "breakdown": e2e_parts},
             "gpu_launches": args.steps * CHUNK,
             "chunk_ms": {"first": chunk_ms[0], "median": statistics.median(chunk_ms), "last": chunk_ms[-1]},
             "clocks": clk}

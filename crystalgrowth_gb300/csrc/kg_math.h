@@ -403,6 +403,11 @@ KG_HD int kg_idiv_prepare(double b, kg_idivc* c)
     return 0;
 }
 
+/* 1: subnormal dividends of kg_idiv stay on the integer pipes; 0: they take the hardware division */
+#ifndef KG_IDIV_SUBN
+#define KG_IDIV_SUBN 1
+#endif
+
 /*
  * sign | RN(Q 2^(e-1075)) for a quotient whose exact significand is Q = q + rem/B
  * (q in [2^52, 2^53), rem in [0, B)) and whose biased exponent e < 1: a
@@ -428,6 +433,10 @@ KG_HD double kg_idiv(double a, const kg_idivc* c)
     if (ea == 0x7ff)
         return a / c->b;
     uint64_t A;
+#if KG_IDIV_SUBN == 0
+    if (ea == 0)
+        return a / c->b;
+#endif
     if (ea == 0) { /* subnormal dividend: normalise its significand */
         int sh = kg_clz64(ua & 0x7fffffffffffffffull) - 11;
         A = (ua & 0x7fffffffffffffffull) << sh;
