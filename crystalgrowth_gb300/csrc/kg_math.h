@@ -145,6 +145,39 @@ KG_HD uint32_t kg_fbits(float x)
 #endif
 }
 
+/*
+ * The rare FP64 fallbacks of the integer-pipe routines (special operands,
+ * overflow) call these.  On the device they are out-of-line functions:
+ * inlined, the compiler hoisted the first FP64 instruction of a fallback into
+ * the common path, one FP64-pipe instruction per call (measured with ncu on
+ * sm_103a); out of line, the common path carries none.  Same IEEE operations.
+ */
+#ifndef KG_SLOW_NOINLINE
+#define KG_SLOW_NOINLINE 1
+#endif
+#if defined(__CUDA_ARCH__) && KG_SLOW_NOINLINE
+__device__ __noinline__ static double kg_div_slow_dev(double a, double b) { return a / b; }
+__device__ __noinline__ static double kg_add_slow_dev(double a, double b) { return a + b; }
+#endif
+
+KG_HD double kg_div_slow(double a, double b)
+{
+#if defined(__CUDA_ARCH__) && KG_SLOW_NOINLINE
+    return kg_div_slow_dev(a, b);
+#else
+    return a / b;
+#endif
+}
+
+KG_HD double kg_add_slow(double a, double b)
+{
+#if defined(__CUDA_ARCH__) && KG_SLOW_NOINLINE
+    return kg_add_slow_dev(a, b);
+#else
+    return a + b;
+#endif
+}
+
 /* correctly rounded FP32 reciprocal (the same bits on host and device) */
 KG_HD float kg_rcp_f(float x)
 {
@@ -192,7 +225,7 @@ KG_HD double kg_atan_f64(double x)
     double ax = kg_from_bits(ua);
     if (ua > 0x43f0000000000000ull) {          /* |x| > 2^64, inf or NaN */
         if (ua > 0x7ff0000000000000ull)
-            return x + x;
+            return kg_add_slow(x, x);
         return (ux >> 63) ? -KG_PIO2_HI : KG_PIO2_HI;
     }
     double t, tlo = 0.0;
@@ -323,7 +356,7 @@ KG_HD double kg_cdiv(double a, double b, double yh, double yl)
         if (sh == 0 || ((uq >> 52) & 0x7ff) > 200u)
             return kg_from_bits(uq - sh);
     }
-    return a / b;
+    return kg_div_slow(a, b);
 }
 
 
@@ -352,10 +385,22 @@ typedef struct kg_idivc {
     int pow2;    /* b is a power of two */
 } kg_idivc;
 
+/* 1: kg_clz64 from two 32-bit counts on the device; 0: the 64-bit intrinsic */
+#ifndef KG_CLZ32
+#define KG_CLZ32 1
+#endif
+
 KG_HD int kg_clz64(uint64_t x)
 {
 #if defined(__CUDA_ARCH__)
+#if KG_CLZ32
+    /* two 32-bit counts on the integer pipe; the 64-bit count measured one FP64-pipe instruction
+     * per call on sm_103a */
+    uint32_t hi = (uint32_t)(x >> 32);
+    return hi ? __clz((int)hi) : 32 + __clz((int)(uint32_t)x);
+#else
     return __clzll((long long)x);
+#endif
 #else
     return x ? __builtin_clzll(x) : 64;
 #endif
@@ -423,19 +468,28 @@ KG_HD double kg_round_subnormal(uint64_t sign, uint64_t q, uint64_t rem, int e)
     return kg_from_bits(sign | m);
 }
 
+/* 1: the dividend is made opaque to the compiler on entry (an empty asm), so that it is kept in a
+ * register instead of being recomputed from its FP64 operands around the integer sequence */
+#ifndef KG_IDIV_OPAQUE
+#define KG_IDIV_OPAQUE 1
+#endif
+
 KG_HD double kg_idiv(double a, const kg_idivc* c)
 {
+#if KG_IDIV_OPAQUE && defined(__CUDA_ARCH__)
+    asm volatile("" : "+d"(a));
+#endif
     uint64_t ua = kg_bits(a);
     uint64_t sign = ua & 0x8000000000000000ull;
     int ea = (int)((ua >> 52) & 0x7ff);
     if ((ua & 0x7fffffffffffffffull) == 0)
         return a;
     if (ea == 0x7ff)
-        return a / c->b;
+        return kg_div_slow(a, c->b);
     uint64_t A;
 #if KG_IDIV_SUBN == 0
     if (ea == 0)
-        return a / c->b;
+        return kg_div_slow(a, c->b);
 #endif
     if (ea == 0) { /* subnormal dividend: normalise its significand */
         int sh = kg_clz64(ua & 0x7fffffffffffffffull) - 11;
@@ -465,7 +519,7 @@ KG_HD double kg_idiv(double a, const kg_idivc* c)
         if (e < 1)
             return kg_round_subnormal(sign, q, rem, e);
     }
-    return a / c->b;
+    return kg_div_slow(a, c->b);
 }
 
 
@@ -482,7 +536,7 @@ KG_HD double kg_iadd(double a, double b)
     uint64_t ua = kg_bits(a), ub = kg_bits(b);
     uint64_t aa = ua & 0x7fffffffffffffffull, ab = ub & 0x7fffffffffffffffull;
     if (aa >= 0x7ff0000000000000ull || ab >= 0x7ff0000000000000ull)
-        return a + b;
+        return kg_add_slow(a, b);
     int swap = ab > aa;
     uint64_t ux = swap ? ub : ua, uy = swap ? ua : ub;
     uint64_t ax = swap ? ab : aa, ay = swap ? aa : ab;
@@ -534,7 +588,7 @@ KG_HD double kg_imul2(double x)
     uint64_t u = kg_bits(x);
     uint64_t a = u & 0x7fffffffffffffffull;
     if (a >= 0x7fe0000000000000ull)
-        return x + x;
+        return kg_add_slow(x, x);
     if (a < 0x0010000000000000ull)
         return kg_from_bits((u & 0x8000000000000000ull) | (a << 1));
     return kg_from_bits(u + 0x0010000000000000ull);
@@ -618,12 +672,15 @@ KG_HD uint64_t kg_recip116(uint64_t B)
  */
 KG_HD double kg_gdiv(double a, double b)
 {
+#if KG_IDIV_OPAQUE && defined(__CUDA_ARCH__)
+    asm volatile("" : "+d"(a), "+d"(b));
+#endif
     const uint64_t MANT = 0x000fffffffffffffull, HID = 0x0010000000000000ull;
     uint64_t ua = kg_bits(a), ub = kg_bits(b);
     uint64_t sign = (ua ^ ub) & 0x8000000000000000ull;
     int ea = (int)((ua >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff);
     if (eb == 0x7ff || ea == 0x7ff || (ub & 0x7fffffffffffffffull) == 0)
-        return a / b;
+        return kg_div_slow(a, b);
     if ((ua & 0x7fffffffffffffffull) == 0)
         return kg_from_bits(sign);
     uint64_t A, B;
@@ -647,7 +704,7 @@ KG_HD double kg_gdiv(double a, double b)
             return kg_from_bits(sign | ((uint64_t)e << 52) | (A & MANT));
         if (e < 1)
             return kg_round_subnormal(sign, A, 0, e);
-        return a / b;
+        return kg_div_slow(a, b);
     }
     uint64_t R = kg_recip116(B);
     int shift = A < B;
@@ -667,7 +724,7 @@ KG_HD double kg_gdiv(double a, double b)
         return kg_from_bits(sign | (((uint64_t)(e - 1) << 52) + q + ((uint64_t)r * 2 > B)));
     if (e < 1)
         return kg_round_subnormal(sign, q, (uint64_t)r, e);
-    return a / b;
+    return kg_div_slow(a, b);
 }
 
 /* ---- elementary functions on the integer pipes (fixed point) ----
@@ -733,7 +790,7 @@ KG_HD double kg_atan_x(double x)
     uint64_t sign = ux & 0x8000000000000000ull;
     if (ua > 0x43f0000000000000ull) { /* |x| > 2^64, inf or NaN */
         if (ua > 0x7ff0000000000000ull)
-            return x + x;
+            return kg_add_slow(x, x);
         return kg_from_bits(sign | kg_bits(KG_PIO2_HI));
     }
     if (ua < 0x3e40000000000000ull) /* |x| < 2^-27 */
@@ -790,6 +847,20 @@ KG_HD double kg_atan_x(double x)
     return kg_from_bits(kg_bits(r) | sign);
 }
 
+/* kg_sincos_f64 out of line on the device (see kg_div_slow) */
+#if defined(__CUDA_ARCH__) && KG_SLOW_NOINLINE
+__device__ __noinline__ static void kg_sincos_slow_dev(double x, double* s, double* c) { kg_sincos_f64(x, s, c); }
+#endif
+
+KG_HD void kg_sincos_slow(double x, double* s_out, double* c_out)
+{
+#if defined(__CUDA_ARCH__) && KG_SLOW_NOINLINE
+    kg_sincos_slow_dev(x, s_out, c_out);
+#else
+    kg_sincos_f64(x, s_out, c_out);
+#endif
+}
+
 /*
  * sin(x) and cos(x) on the integer pipes for |x| < 64; larger |x| (and inf,
  * NaN) take kg_sincos_f64.
@@ -809,7 +880,7 @@ KG_HD void kg_sincos_x(double x, double* s_out, double* c_out)
     const uint64_t MANT = 0x000fffffffffffffull, HID = 0x0010000000000000ull;
     uint64_t ux = kg_bits(x), ua = ux & 0x7fffffffffffffffull;
     if (ua >= 0x4050000000000000ull) { /* |x| >= 64, inf, NaN */
-        kg_sincos_f64(x, s_out, c_out);
+        kg_sincos_slow(x, s_out, c_out);
         return;
     }
     if (ua < 0x3e40000000000000ull) { /* |x| < 2^-27 */
