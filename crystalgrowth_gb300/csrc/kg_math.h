@@ -102,9 +102,21 @@ KG_HD int64_t kg_tab_scx(int i)
 #endif
 }
 
+/* 1: on the device the bit pattern comes through an inline-PTX move, which the optimiser cannot see
+ * through; with a plain reinterpretation it may turn a test such as (bits & ~sign) == 0 or
+ * (bits & ~sign) <= c back into a floating-point comparison, which on sm_103a runs on the narrow
+ * FP64 pipe (measured: one FP64-pipe instruction per such test) */
+#ifndef KG_BITS_ASM
+#define KG_BITS_ASM 1
+#endif
+
 KG_HD uint64_t kg_bits(double x)
 {
-#if defined(__CUDA_ARCH__)
+#if defined(__CUDA_ARCH__) && KG_BITS_ASM
+    uint64_t u;
+    asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+    return u;
+#elif defined(__CUDA_ARCH__)
     return (uint64_t)__double_as_longlong(x);
 #else
     uint64_t u;
