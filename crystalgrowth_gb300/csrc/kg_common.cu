@@ -184,12 +184,20 @@ int kg_prepare(const kg_params* p, KgDev* d)
     return KG_OK;
 }
 
-/* Strip shape for one grid: the largest strips that still give the GPU about
- * 30,000 CTAs (measured on GB300: below that, strips covering the growing
- * crystals finish last and the SMs idle; above it, the repeated halo rows of
- * short strips cost more than they save), down to one-warp strips of 4 rows. */
+/* Strip shape for one grid.  Strips of 128 x 16 wherever they give at least
+ * 8,000 CTAs, about 8 waves (measured on GB300 with the current step: best at
+ * 4096^2 and 8192^2, e.g. 1.01e10 against 8.2e9 for 64 x 8 late in the
+ * 4096^2 trajectory).  Smaller grids: the largest strips that still give
+ * about 30,000 CTAs (below that, strips covering the growing crystals finish
+ * last and the SMs idle; above it, the repeated halo rows of short strips cost
+ * more than they save), down to one-warp strips of 4 rows. */
 void kg_pick_tile(int nx, int ny, int* nt, int* bh)
 {
+    if ((long long)((nx + 125) / 126) * ((ny + 15) / 16) >= 8000) {
+        *nt = 128;
+        *bh = 16 < ny ? 16 : ny;
+        return;
+    }
     const long long want = 30000;
     const int shapes[8][2] = {{128, 64}, {128, 32}, {128, 16}, {64, 16}, {64, 8}, {32, 8}, {32, 4}};
     for (int k = 0; k < 7; k++) {
