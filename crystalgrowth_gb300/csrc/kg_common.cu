@@ -10,10 +10,13 @@ static thread_local char g_err[512];
 
 int kg_fail(int code, const char* fmt, ...)
 {
+    /* formatted into a local buffer first: a caller may pass kg_last_error() itself as an argument */
+    char buf[sizeof g_err];
     va_list ap;
     va_start(ap, fmt);
-    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    vsnprintf(buf, sizeof buf, fmt, ap);
     va_end(ap);
+    memcpy(g_err, buf, sizeof g_err);
     return code;
 }
 

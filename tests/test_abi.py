@@ -111,3 +111,18 @@ def test_slider_model():
     bad[4] = 10
     assert lib.kg_params_from_sliders(bad, 1e-4, ctypes.byref(p)) == _lib.KG_ERR_INVALID
     assert b"outside" in lib.kg_last_error()
+
+
+def test_batch_create_reports_the_failing_instance_without_a_gpu():
+    """kg_batch_create validates every instance before touching the device; the message names the
+    instance and carries the parameter check's own text (formatted from the previous message)"""
+    lib = kg.load()
+    n = 3
+    nx = (ctypes.c_int * n)(64, 80, 96)
+    ny = (ctypes.c_int * n)(64, 80, 96)
+    params = (kg.Params * n)(kg.Params.make(), kg.Params.make(tau=0.0), kg.Params.make())
+    out = ctypes.c_void_p()
+    assert lib.kg_batch_create(n, nx, ny, params, ctypes.byref(out)) == _lib.KG_ERR_INVALID
+    msg = lib.kg_last_error().decode()
+    assert msg.startswith("kg_batch_create: instance 1: params:"), msg
+    assert not out.value
