@@ -556,6 +556,13 @@ extern "C" int kg_load(kg_sim* h, const char* path)
         return rc;
     }
     size_t cells = (size_t)nx * ny;
+    /* the whole payload must be present before anything reaches the device: a short file leaves the
+     * handle as it was */
+    if (fseek(f, 0, SEEK_END) != 0 || ftell(f) != (long)(KG_SNAP_HEADER + 3 * cells * sizeof(double)) ||
+        fseek(f, KG_SNAP_HEADER, SEEK_SET) != 0) {
+        fclose(f);
+        return kg_fail(KG_ERR_INVALID, "kg_load: %s is truncated or too long for %lld x %lld", path, nx, ny);
+    }
     double* buf = (double*)malloc(cells * sizeof(double));
     if (!buf) {
         fclose(f);

@@ -67,6 +67,14 @@ def test_snapshot_roundtrip_and_format(tmp_path):
     b.step(77)
     for x, y in zip(a.fields(), b.fields()):
         assert np.array_equal(x.view(np.uint64), y.view(np.uint64))
+    # a truncated snapshot is rejected before any field reaches the device: the handle is unchanged
+    short = tmp_path / "short.kgs"
+    short.write_bytes(raw[:-8])
+    before = b.fields()
+    with pytest.raises(KgError):
+        b.load(short)
+    for x, y in zip(before, b.fields()):
+        assert np.array_equal(x.view(np.uint64), y.view(np.uint64))
     c = Kobayashi(91, 70, 1e-4)
     with pytest.raises(KgError):
         c.load(path)
