@@ -15,7 +15,7 @@
  *
  * The arithmetic reproduces the reference operation for operation in IEEE
  * FP64 (this file is compiled with -fmad=false, so a*b+c is never fused
- * unless written as kg_fma), with three exact shortcuts:
+ * unless written as kg_fma), with these exact shortcuts:
  *   - divisions by dx, dy, 3 dx^2 and tau use kg_idiv: the IEEE quotient's
  *     bits from 64-bit integer arithmetic, off the FP64 pipe; the angle's
  *     gy/gx uses kg_gdiv, the same for a divisor that varies per cell;
@@ -33,7 +33,10 @@
  *     are settled on bit patterns;
  *   - for |phi| <= 2^-56 the double well phi (1 - phi) (phi - 0.5 + m) is
  *     exactly phi (m - 0.5): the other factors round to 1 and -0.5.
- * Comparisons use the bit patterns (integer pipe), never the FP64 pipe.
+ * Comparisons use the bit patterns (integer pipe), never the FP64 pipe: kg_bits
+ * takes them through an inline-PTX move, so the optimiser cannot turn a bit
+ * test back into an FP64 comparison.  atan, sin and cos (kg_math.h) run on
+ * the integer pipes as well.
  */
 #pragma once
 #include <stdint.h>
