@@ -342,6 +342,8 @@ def run_ours(args, rank, world):
     sim.set_graph_chunk(CHUNK)
     if args.tile:
         sim.set_tile(*(int(v) for v in args.tile.split(",")))
+    if args.tblock != 1:
+        sim.set_tblock(args.tblock)
     stream = torch.cuda.ExternalStream(sim.stream())
 
     # warm-up chunks (graph build, clocks), then the state is re-seeded: the timed chunks are time
@@ -450,6 +452,7 @@ def run_ours(args, rank, world):
                        "e2e_steps": "%d chunks continuing from the timed run's final state, after one untimed "
                                     "round trip" % e2e_steps,
                        "strips": "%d threads x %d rows" % sim.tile(),
+                       "tblock": sim.tblock(),
                        "l2": "inputs larger than L2 (3.2 GB state)", "parallelism": "replicas" if world > 1 else "1 GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
@@ -484,6 +487,7 @@ def main():
     ap.add_argument("--disks", type=int, default=64)
     ap.add_argument("--tile", default="", help="strip shape NT,BH (default: the library's choice for the grid)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (short profiling runs)")
+    ap.add_argument("--tblock", type=int, default=1, help="time steps per pass over HBM (1, or 2: temporal blocking)")
     args = ap.parse_args()
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":

@@ -77,6 +77,8 @@ _SIGS = {
     "kg_load": [_vp, ctypes.c_char_p],
     "kg_colormap_device": [_vp, ctypes.c_int, _vp],
     "kg_get_tile": [_vp, _ip, _ip],
+    "kg_set_tblock": [_vp, ctypes.c_int],
+    "kg_get_tblock": [_vp, _ip],
     "kg_step_noalloc": [ctypes.c_int, ctypes.c_int, ctypes.POINTER(Params), _vp, _vp, _vp, ctypes.c_longlong, _vp],
     "kg_last_error": [],
     "kg_version": [],
@@ -105,6 +107,9 @@ _SIGS = {
     "kg_adjoint_gradient": [_vp, _vp, _dp],
     "kg_adjoint_get_stream": [_vp, ctypes.POINTER(_vp)],
     "kg_diag_fp64_peak": [ctypes.POINTER(ctypes.c_double)],
+    "kg_diag_fp64_probe": [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                           ctypes.POINTER(ctypes.c_double)],
+    "kg_diag_inject_timeout": [_vp],
 }
 _RESTYPE = {"kg_last_error": ctypes.c_char_p, "kg_version": ctypes.c_char_p}
 

@@ -11,7 +11,7 @@ KG_BATCH_PERSISTENT = 1
 
 class Tuning(ctypes.Structure):
     _fields_ = [("nt", ctypes.c_int), ("bh", ctypes.c_int), ("mode", ctypes.c_int), ("chunk", ctypes.c_int),
-                ("streams", ctypes.c_int)]
+                ("streams", ctypes.c_int), ("tblock", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -64,8 +64,9 @@ class Batch:
         check(lib().kg_batch_get_tuning(self._h, ctypes.byref(t)))
         return t.as_dict()
 
-    def set_tuning(self, nt=128, bh=64, mode=KG_BATCH_LAUNCH, chunk=100, streams=1):
-        t = Tuning(nt, bh, mode, chunk, streams)
+    def set_tuning(self, nt=128, bh=64, mode=KG_BATCH_LAUNCH, chunk=100, streams=1, tblock=1):
+        """tblock: time steps per pass over HBM (1, or 2 for temporal blocking)"""
+        t = Tuning(nt, bh, mode, chunk, streams, tblock)
         check(lib().kg_batch_set_tuning(self._h, ctypes.byref(t)))
 
     def autotune(self, trial_steps=5):

@@ -21,6 +21,7 @@
  */
 #include <algorithm>
 #include <new>
+#include <type_traits>
 #include <string.h>
 #include <vector>
 #include "kg_common.h"
@@ -52,7 +53,9 @@ __device__ __forceinline__ void kg_inst_ptrs(const KgInst& in, double* arena, in
     dst[2] = b + 2 * n;
 }
 
-template <int NT>
+/* one strip of the work list.  COH: the persistent kernel, whose CTAs read in step s+1 what other CTAs
+ * wrote in step s of the same launch, loads the fields through L2 only */
+template <int NT, bool COH>
 __device__ __forceinline__ void kg_batch_item(const int4 w, const KgDev* __restrict__ P, const KgInst* __restrict__ I,
                                               double* arena, int from, int bh, KgSmem<NT>& sm)
 {
@@ -60,15 +63,33 @@ __device__ __forceinline__ void kg_batch_item(const int4 w, const KgDev* __restr
     const double* s[3];
     double* d[3];
     kg_inst_ptrs(in, arena, from, s, d);
-    kg_strip<NT>(P[w.x], in.nx, in.ny, s[0], s[1], s[2], d[0], d[1], d[2], w.y, w.z, bh, sm);
+    kg_strip<NT, false, COH>(P[w.x], in.nx, in.ny, s[0], s[1], s[2], d[0], d[1], d[2], w.y, w.z, bh, sm);
 }
 
-template <int NT>
+/* the same with temporal blocking: two steps per pass (kg_strip2) */
+template <int NT, bool COH>
+__device__ __forceinline__ void kg_batch_item2(const int4 w, const KgDev* __restrict__ P, const KgInst* __restrict__ I,
+                                               double* arena, int from, int bh, KgSmem2<NT>& sm)
+{
+    const KgInst in = I[w.x];
+    const double* s[3];
+    double* d[3];
+    kg_inst_ptrs(in, arena, from, s, d);
+    kg_strip2<NT, COH>(P[w.x], in.nx, in.ny, s[0], s[1], s[2], d[0], d[1], d[2], w.y, w.z, bh, sm);
+}
+
+/* one strip per CTA; K = 1 or 2 time steps */
+template <int NT, int K>
 __global__ void __launch_bounds__(NT) kg_batch_step_kernel(const int4* __restrict__ work, const KgDev* __restrict__ P,
                                                            const KgInst* __restrict__ I, double* arena, int from, int bh)
 {
-    __shared__ KgSmem<NT> sm;
-    kg_batch_item<NT>(work[blockIdx.x], P, I, arena, from, bh, sm);
+    if constexpr (K == 2) {
+        __shared__ KgSmem2<NT> sm;
+        kg_batch_item2<NT, false>(work[blockIdx.x], P, I, arena, from, bh, sm);
+    } else {
+        __shared__ KgSmem<NT> sm;
+        kg_batch_item<NT, false>(work[blockIdx.x], P, I, arena, from, bh, sm);
+    }
 }
 
 /* bounded grid barrier; returns false when the wait ran out (or another CTA's did) */
@@ -103,21 +124,25 @@ __device__ bool kg_grid_barrier(KgBarrier* bar, unsigned nblocks, long long max_
     return ok != 0;
 }
 
-template <int NT>
+/* nlaunch passes of K (1 or 2) time steps each, separated by grid barriers */
+template <int NT, int K>
 __global__ void __launch_bounds__(NT) kg_batch_persistent_kernel(const int4* __restrict__ work, int nwork,
                                                                  const KgDev* __restrict__ P,
                                                                  const KgInst* __restrict__ I, double* arena, int from,
-                                                                 int bh, int nsteps, KgBarrier* bar,
+                                                                 int bh, int nlaunch, KgBarrier* bar,
                                                                  long long max_polls)
 {
-    __shared__ KgSmem<NT> sm;
-    for (int s = 0; s < nsteps; s++) {
+    __shared__ typename std::conditional<K == 2, KgSmem2<NT>, KgSmem<NT>>::type sm;
+    for (int s = 0; s < nlaunch; s++) {
         for (int k = blockIdx.x; k < nwork; k += gridDim.x) {
-            kg_batch_item<NT>(work[k], P, I, arena, from, bh, sm);
+            if constexpr (K == 2)
+                kg_batch_item2<NT, true>(work[k], P, I, arena, from, bh, sm);
+            else
+                kg_batch_item<NT, true>(work[k], P, I, arena, from, bh, sm);
             __syncthreads();
         }
         from ^= 1;
-        if (s + 1 < nsteps && !kg_grid_barrier(bar, gridDim.x, max_polls))
+        if (s + 1 < nlaunch && !kg_grid_barrier(bar, gridDim.x, max_polls))
             return;
     }
 }
@@ -136,7 +161,7 @@ struct kg_batch {
     cudaStream_t stream = nullptr;
     int cur = 0;
     long long steps = 0;
-    kg_batch_tuning tune{128, 64, KG_BATCH_LAUNCH, 100, 1};
+    kg_batch_tuning tune{128, 64, KG_BATCH_LAUNCH, 100, 1, 1};
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long cells = 0;
     /* launch mode with tune.streams > 1: the instances are split into groups of about equal cell
@@ -146,10 +171,20 @@ struct kg_batch {
     cudaStream_t gs[KG_BATCH_MAX_STREAMS] = {nullptr};
     cudaEvent_t fork_ev = nullptr;
     cudaEvent_t join_ev[KG_BATCH_MAX_STREAMS] = {nullptr};
+    /* set when a grid-barrier wait ran out: kg_batch_step refuses until every instance's state has been
+     * replaced since (kg_batch_seed_disks or kg_batch_set_fields with all three fields) */
+    bool failed = false;
+    std::vector<char> replaced;
 };
 
+/* Destroys the instantiated graphs after draining the handle's stream (a graph launched earlier may
+ * still be running). */
 static void batch_drop_graphs(kg_batch* b)
 {
+    if (!b->graph[0] && !b->graph[1])
+        return;
+    if (b->stream)
+        cudaStreamSynchronize(b->stream);
     for (int k = 0; k < 2; k++)
         if (b->graph[k]) {
             cudaGraphExecDestroy(b->graph[k]);
@@ -176,6 +211,10 @@ static int valid_tuning(const kg_batch_tuning* t)
         return kg_fail(KG_ERR_INVALID, "batch tuning: chunk must lie in [1, 100000]");
     if (t->streams < 1 || t->streams > KG_BATCH_MAX_STREAMS)
         return kg_fail(KG_ERR_INVALID, "batch tuning: streams must lie in [1, %d]", KG_BATCH_MAX_STREAMS);
+    if (t->tblock != 1 && t->tblock != 2)
+        return kg_fail(KG_ERR_INVALID, "batch tuning: tblock (steps per pass) must be 1 or 2");
+    if (t->tblock == 2 && t->nt > 128)
+        return kg_fail(KG_ERR_INVALID, "batch tuning: tblock 2 needs nt <= 128");
     return KG_OK;
 }
 
@@ -199,7 +238,7 @@ static int build_work(kg_batch* b)
         load[g] += cells(k);
     }
     std::vector<int4> w;
-    const int cw = b->tune.nt - 2;
+    const int cw = b->tune.nt - 2 - 4 * (b->tune.tblock - 1); /* output columns per strip */
     for (int g = 0; g < ng; g++) {
         b->goff[g] = (int)w.size();
         for (int k : groups[g]) {
@@ -228,25 +267,53 @@ static int build_work(kg_batch* b)
     return KG_OK;
 }
 
-template <int NT>
+template <int NT, int K>
 static cudaError_t launch_range(kg_batch* b, int first, int count, int from, cudaStream_t st)
 {
-    kg_batch_step_kernel<NT><<<count, NT, 0, st>>>(b->d_work + first, b->d_params, b->d_inst, b->arena, from,
-                                                   b->tune.bh);
+    kg_batch_step_kernel<NT, K><<<count, NT, 0, st>>>(b->d_work + first, b->d_params, b->d_inst, b->arena, from,
+                                                      b->tune.bh);
     return cudaGetLastError();
 }
 
-static cudaError_t launch_group(kg_batch* b, int g, int from, cudaStream_t st)
+/* one launch of group g advancing k (1 or 2) steps from copy `from` */
+static cudaError_t launch_group(kg_batch* b, int g, int from, int k, cudaStream_t st)
 {
     int first = b->goff[g], count = b->goff[g + 1] - b->goff[g];
     if (count <= 0)
         return cudaSuccess;
-    switch (b->tune.nt) {
-    case 32: return launch_range<32>(b, first, count, from, st);
-    case 64: return launch_range<64>(b, first, count, from, st);
-    case 256: return launch_range<256>(b, first, count, from, st);
-    default: return launch_range<128>(b, first, count, from, st);
+    if (k == 2) {
+        switch (b->tune.nt) {
+        case 32: return launch_range<32, 2>(b, first, count, from, st);
+        case 64: return launch_range<64, 2>(b, first, count, from, st);
+        default: return launch_range<128, 2>(b, first, count, from, st);
+        }
     }
+    switch (b->tune.nt) {
+    case 32: return launch_range<32, 1>(b, first, count, from, st);
+    case 64: return launch_range<64, 1>(b, first, count, from, st);
+    case 256: return launch_range<256, 1>(b, first, count, from, st);
+    default: return launch_range<128, 1>(b, first, count, from, st);
+    }
+}
+
+/* launches that advance n steps with the tuning's temporal blocking factor */
+static long long batch_launches_for(const kg_batch* b, long long n)
+{
+    return b->tune.tblock == 2 ? n / 2 + (n & 1) : n;
+}
+
+/* n steps of group g from copy `from` on stream st: k = 2 launches, then a k = 1 launch for an odd rest */
+static cudaError_t launch_group_steps(kg_batch* b, int g, int from, long long n, cudaStream_t st)
+{
+    cudaError_t e = cudaSuccess;
+    int c = from;
+    for (long long s = 0; s < n && e == cudaSuccess;) {
+        const int k = (b->tune.tblock == 2 && n - s >= 2) ? 2 : 1;
+        e = launch_group(b, g, c, k, st);
+        c ^= 1;
+        s += k;
+    }
+    return e;
 }
 
 /* nsteps consecutive steps from copy `from`: on the handle's stream, or forked
@@ -255,14 +322,13 @@ static int batch_launch_steps(kg_batch* b, int from, int nsteps)
 {
     cudaError_t e = cudaSuccess;
     if (b->ngroups <= 1) {
-        for (int s = 0; s < nsteps && e == cudaSuccess; s++)
-            e = launch_group(b, 0, from ^ (s & 1), b->stream);
+        e = launch_group_steps(b, 0, from, nsteps, b->stream);
     } else {
         e = cudaEventRecord(b->fork_ev, b->stream);
         for (int g = 0; g < b->ngroups && e == cudaSuccess; g++) {
             e = cudaStreamWaitEvent(b->gs[g], b->fork_ev, 0);
-            for (int s = 0; s < nsteps && e == cudaSuccess; s++)
-                e = launch_group(b, g, from ^ (s & 1), b->gs[g]);
+            if (e == cudaSuccess)
+                e = launch_group_steps(b, g, from, nsteps, b->gs[g]);
             if (e == cudaSuccess)
                 e = cudaEventRecord(b->join_ev[g], b->gs[g]);
             if (e == cudaSuccess)
@@ -274,8 +340,8 @@ static int batch_launch_steps(kg_batch* b, int from, int nsteps)
     return KG_OK;
 }
 
-template <int NT>
-static int persistent_run(kg_batch* b, int from, int nsteps)
+template <int NT, int K>
+static int persistent_run(kg_batch* b, int from, int nlaunch)
 {
     int dev = 0, sms = 0, per_sm = 0, coop = 0;
     KG_CUDA(cudaGetDevice(&dev));
@@ -283,25 +349,33 @@ static int persistent_run(kg_batch* b, int from, int nsteps)
     KG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (!coop)
         return kg_fail(KG_ERR_CUDA, "persistent batch mode needs cooperative launch support");
-    KG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kg_batch_persistent_kernel<NT>, NT, 0));
+    KG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kg_batch_persistent_kernel<NT, K>, NT, 0));
     int grid = std::min(b->nwork, std::max(1, per_sm) * sms);
     /* a wait longer than ~2 s means a CTA is missing: report instead of hanging */
     long long max_polls = 8ll << 20;
     KG_CUDA(cudaMemsetAsync(b->d_bar, 0, sizeof(KgBarrier), b->stream));
     void* args[] = {(void*)&b->d_work, (void*)&b->nwork, (void*)&b->d_params, (void*)&b->d_inst, (void*)&b->arena,
-                    (void*)&from, (void*)&b->tune.bh, (void*)&nsteps, (void*)&b->d_bar, (void*)&max_polls};
-    KG_CUDA(cudaLaunchCooperativeKernel((const void*)kg_batch_persistent_kernel<NT>, dim3(grid), dim3(NT), args, 0,
+                    (void*)&from, (void*)&b->tune.bh, (void*)&nlaunch, (void*)&b->d_bar, (void*)&max_polls};
+    KG_CUDA(cudaLaunchCooperativeKernel((const void*)kg_batch_persistent_kernel<NT, K>, dim3(grid), dim3(NT), args, 0,
                                         b->stream));
     return KG_OK;
 }
 
-static int batch_persistent(kg_batch* b, int from, int nsteps)
+/* one persistent launch of nlaunch passes of k steps each from copy `from` */
+static int batch_persistent(kg_batch* b, int from, int nlaunch, int k)
 {
+    if (k == 2) {
+        switch (b->tune.nt) {
+        case 32: return persistent_run<32, 2>(b, from, nlaunch);
+        case 64: return persistent_run<64, 2>(b, from, nlaunch);
+        default: return persistent_run<128, 2>(b, from, nlaunch);
+        }
+    }
     switch (b->tune.nt) {
-    case 32: return persistent_run<32>(b, from, nsteps);
-    case 64: return persistent_run<64>(b, from, nsteps);
-    case 256: return persistent_run<256>(b, from, nsteps);
-    default: return persistent_run<128>(b, from, nsteps);
+    case 32: return persistent_run<32, 1>(b, from, nlaunch);
+    case 64: return persistent_run<64, 1>(b, from, nlaunch);
+    case 256: return persistent_run<256, 1>(b, from, nlaunch);
+    default: return persistent_run<128, 1>(b, from, nlaunch);
     }
 }
 
@@ -333,9 +407,22 @@ static int batch_check_barrier(kg_batch* b)
     KgBarrier h;
     KG_CUDA(cudaMemcpyAsync(&h, b->d_bar, sizeof h, cudaMemcpyDeviceToHost, b->stream));
     KG_CUDA(cudaStreamSynchronize(b->stream));
-    if (h.err)
+    if (h.err) {
+        b->failed = true;
+        std::fill(b->replaced.begin(), b->replaced.end(), 0);
         return kg_fail(KG_ERR_TIMEOUT, "batch: a grid-barrier wait ran out; the chunk did not complete");
+    }
     return KG_OK;
+}
+
+/* instance k's state was replaced: the time-out latch clears once every instance's has been */
+static void batch_replaced(kg_batch* b, int k)
+{
+    if (!b->failed)
+        return;
+    b->replaced[k] = 1;
+    if (std::all_of(b->replaced.begin(), b->replaced.end(), [](char c) { return c != 0; }))
+        b->failed = false;
 }
 
 extern "C" int kg_batch_step(kg_batch* b, long long nsteps)
@@ -345,17 +432,27 @@ extern "C" int kg_batch_step(kg_batch* b, long long nsteps)
         return rc;
     if (nsteps < 0)
         return kg_fail(KG_ERR_INVALID, "kg_batch_step: negative step count");
+    if (b->failed)
+        return kg_fail(KG_ERR_TIMEOUT, "kg_batch_step: an earlier grid-barrier wait ran out and the state is "
+                                       "unreliable; replace it first (kg_batch_seed_disks / kg_batch_set_fields on "
+                                       "every instance)");
     if (b->tune.mode == KG_BATCH_PERSISTENT) {
         while (nsteps > 0) {
             int s = (int)std::min<long long>(nsteps, b->tune.chunk);
-            rc = batch_persistent(b, b->cur, s);
-            if (rc)
-                return rc;
-            rc = batch_check_barrier(b);
-            if (rc)
-                return rc;
-            if (s & 1)
-                b->cur ^= 1;
+            /* passes of tblock steps in one launch, then a one-step launch for an odd rest */
+            const int k = b->tune.tblock;
+            const int passes[2] = {s / k, s % k};
+            for (int part = 0; part < 2; part++) {
+                if (passes[part] == 0)
+                    continue;
+                rc = batch_persistent(b, b->cur, passes[part], part == 0 ? k : 1);
+                if (rc)
+                    return rc;
+                rc = batch_check_barrier(b);
+                if (rc)
+                    return rc;
+                b->cur ^= passes[part] & 1;
+            }
             b->steps += s;
             nsteps -= s;
         }
@@ -368,7 +465,7 @@ extern "C" int kg_batch_step(kg_batch* b, long long nsteps)
                 return rc;
         }
         KG_CUDA(cudaGraphLaunch(b->graph[b->cur], b->stream));
-        b->cur ^= (b->tune.chunk & 1);
+        b->cur ^= (int)(batch_launches_for(b, b->tune.chunk) & 1);
         b->steps += b->tune.chunk;
         nsteps -= b->tune.chunk;
     }
@@ -376,7 +473,7 @@ extern "C" int kg_batch_step(kg_batch* b, long long nsteps)
         rc = batch_launch_steps(b, b->cur, (int)nsteps);
         if (rc)
             return rc;
-        b->cur ^= (int)(nsteps & 1);
+        b->cur ^= (int)(batch_launches_for(b, nsteps) & 1);
         b->steps += nsteps;
     }
     return KG_OK;
@@ -386,9 +483,9 @@ extern "C" int kg_batch_destroy(kg_batch* b)
 {
     if (!b)
         return KG_OK;
-    batch_drop_graphs(b);
     if (b->stream)
         cudaStreamSynchronize(b->stream);
+    batch_drop_graphs(b);
     cudaFree(b->arena);
     cudaFree(b->d_params);
     cudaFree(b->d_inst);
@@ -421,6 +518,7 @@ extern "C" int kg_batch_create(int n, const int* nx, const int* ny, const kg_par
         return kg_fail(KG_ERR_NOMEM, "kg_batch_create: host allocation");
     b->n = n;
     b->inst.resize(n);
+    b->replaced.assign(n, 0);
     b->params.assign(params, params + n);
     long long off = 0;
     for (int k = 0; k < n; k++) {
@@ -501,7 +599,10 @@ extern "C" int kg_batch_seed_disks(kg_batch* b, int k, int n, const int* cx, con
     const KgInst& in = b->inst[k];
     long long cells = (long long)in.nx * in.ny;
     double* a = b->arena + in.off + (long long)b->cur * 3 * cells;
-    return kg_seed_device(a, a + cells, a + 2 * cells, in.nx, in.ny, n, cx, cy, r, b->stream);
+    rc = kg_seed_device(a, a + cells, a + 2 * cells, in.nx, in.ny, n, cx, cy, r, b->stream);
+    if (rc == KG_OK)
+        batch_replaced(b, k);
+    return rc;
 }
 
 extern "C" int kg_batch_get_fields(kg_batch* b, int k, double* phi, double* T, double* theta)
@@ -533,6 +634,8 @@ extern "C" int kg_batch_set_fields(kg_batch* b, int k, const double* phi, const 
         if (src[f])
             KG_CUDA(cudaMemcpyAsync(a + f * cells, src[f], sizeof(double) * cells, cudaMemcpyHostToDevice, b->stream));
     KG_CUDA(cudaStreamSynchronize(b->stream));
+    if (phi && T && theta)
+        batch_replaced(b, k);
     return KG_OK;
 }
 
@@ -564,7 +667,7 @@ extern "C" int kg_batch_set_tuning(kg_batch* b, const kg_batch_tuning* t)
         return rc;
     KG_CUDA(cudaStreamSynchronize(b->stream));
     bool rework = t->nt != b->tune.nt || t->bh != b->tune.bh || t->streams != b->tune.streams ||
-                  t->mode != b->tune.mode;
+                  t->mode != b->tune.mode || t->tblock != b->tune.tblock;
     b->tune = *t;
     batch_drop_graphs(b);
     if (rework)
@@ -622,6 +725,7 @@ extern "C" int kg_batch_autotune(kg_batch* b, int trial_steps, kg_batch_tuning* 
     cudaError_t e = cudaMemcpyAsync(saved, b->arena, bytes, cudaMemcpyDeviceToDevice, b->stream);
     const int saved_cur = b->cur;
     const long long saved_steps = b->steps;
+    const bool saved_failed = b->failed;
     const kg_batch_tuning orig = b->tune;
     kg_batch_tuning best = orig;
     float best_t = 1e30f;
@@ -639,10 +743,13 @@ extern "C" int kg_batch_autotune(kg_batch* b, int trial_steps, kg_batch_tuning* 
     /* (mode, streams): one launch per step; the same over 4, 8 or 16 group streams; persistent */
     const int modes[5][2] = {{KG_BATCH_LAUNCH, 1}, {KG_BATCH_LAUNCH, 4}, {KG_BATCH_LAUNCH, 8}, {KG_BATCH_LAUNCH, 16},
                              {KG_BATCH_PERSISTENT, 1}};
+    /* the temporal blocking factor (steps per pass) sets the halo depth: 2 k rows/columns of phi, k of
+     * T and theta per side */
+    for (int kb = 1; kb <= 2 && rc == KG_OK; kb++)
     for (int mi = 0; mi < 5 && rc == KG_OK; mi++)
         for (int ni = 0; ni < 3 && rc == KG_OK; ni++)
             for (int hi = 0; hi < 4 && rc == KG_OK; hi++) {
-                kg_batch_tuning t{nts[ni], bhs[hi], modes[mi][0], trial_steps, modes[mi][1]};
+                kg_batch_tuning t{nts[ni], bhs[hi], modes[mi][0], trial_steps, modes[mi][1], kb};
                 rc = kg_batch_set_tuning(b, &t);
                 if (rc)
                     break;
@@ -672,9 +779,11 @@ extern "C" int kg_batch_autotune(kg_batch* b, int trial_steps, kg_batch_tuning* 
                     best = t;
                 }
             }
-    /* restore the state and install the winner with the caller's chunk length */
+    /* restore the state and install the winner with the caller's chunk length (a trial that timed out
+     * only ran on a copy: the restored state is the caller's own) */
     b->cur = saved_cur;
     b->steps = saved_steps;
+    b->failed = saved_failed;
     cudaMemcpyAsync(b->arena, saved, bytes, cudaMemcpyDeviceToDevice, b->stream);
     cudaStreamSynchronize(b->stream);
     cudaFree(saved);

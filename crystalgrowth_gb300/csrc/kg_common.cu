@@ -114,9 +114,11 @@ extern "C" int kg_params_from_sliders(const int* pos, double dt, kg_params* p)
 
 static bool finite_all(const kg_params* p)
 {
-    const double* v = &p->dx;
-    for (int i = 0; i < (int)(sizeof(kg_params) / sizeof(double)); i++)
-        if (!isfinite(v[i]))
+    const double v[] = {p->dx, p->dy, p->dt, p->tau, p->eps_bar, p->mu, p->K, p->delta, p->aniso, p->alpha,
+                        p->gamma, p->teq, p->theta0};
+    static_assert(sizeof v == sizeof(kg_params), "every kg_params member is checked");
+    for (double x : v)
+        if (!isfinite(x))
             return false;
     return true;
 }
@@ -181,6 +183,7 @@ int kg_prepare(const kg_params* p, KgDev* d)
     d->u0 = p->gamma * (p->teq - 0.0);
     d->m0 = d->a_pi * kg_atan(d->u0);
     d->t_small = kg_absorb_bound(p->teq);
+    d->zk = kg_bits(p->K * 0.0);
     /* 1 - phi == 1 needs |phi| <= bound(1) = 2^-55, phi - 0.5 == -0.5 needs bound(0.5) = 2^-56 */
     d->phi_small = kg_absorb_bound(0.5);
     d->r0 = -0.5 + d->m0;

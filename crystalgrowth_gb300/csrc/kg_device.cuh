@@ -32,7 +32,13 @@
  *     grad eps^2 . grad phi is a signed zero: its sign, and the sum it joins,
  *     are settled on bit patterns;
  *   - for |phi| <= 2^-56 the double well phi (1 - phi) (phi - 0.5 + m) is
- *     exactly phi (m - 0.5): the other factors round to 1 and -0.5.
+ *     exactly phi (m - 0.5): the other factors round to 1 and -0.5;
+ *   - quiet cells, whose 3x3 phi neighbourhood is all +0 (everywhere the
+ *     front's far tail has not reached): every term of the phi update is a
+ *     signed zero, so phi stays +0 and only T + lap_T dt is computed; with a
+ *     +0 T neighbourhood as well, T stays +0 too.  Stage 1 of a cell whose
+ *     four phi neighbours are +0 keeps theta and takes gx = gy = +0 without
+ *     arithmetic.
  * Comparisons use the bit patterns (integer pipe), never the FP64 pipe: kg_bits
  * takes them through an inline-PTX move, so the optimiser cannot turn a bit
  * test back into an FP64 comparison.  atan, sin and cos (kg_math.h) run on
@@ -53,6 +59,7 @@ struct KgDev {
     double s0, c0;    /* sin(arg0), cos(arg0) */
     double eps0, epsd0, e2_0, ee0; /* eps, eps', eps^2, eps eps' at arg0 */
     double u0, m0;    /* gamma (Teq - 0) and (alpha/pi) atan(u0) */
+    uint64_t zk;      /* bits of K * (+0): the T update's latent-heat term for a quiet cell */
     uint64_t t_small; /* |T| bit patterns up to this leave Teq - T == Teq, so u == u0 */
     uint64_t phi_small; /* |phi| bit patterns up to this leave 1 - phi == 1 and phi - 0.5 == -0.5 */
     double r0;          /* -0.5 + m0: the double-well factor (phi - 0.5 + m) of such a cell */
@@ -71,6 +78,11 @@ __device__ __forceinline__ bool kg_neg_big(uint64_t b)
 {
     return b > (0x8000000000000000ull | KG_EPS_BITS) && b <= 0xfff0000000000000ull;
 }
+
+/* 1: the quiet-cell shortcut (all-zero phi neighbourhoods, exact); 0: the plain sequence everywhere */
+#ifndef KG_QUIET
+#define KG_QUIET 1
+#endif
 
 /* 1: the angle's quotient gy/gx through kg_gdiv (the IEEE bits on the integer pipes); 0: the
  * hardware division */
@@ -105,30 +117,41 @@ struct KgS2Aux {
 __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, double pN, double pS, double& theta)
 {
     KgS1 o;
-    double gx = kg_idiv(pE - pW, &P.idx);
-    double gy = kg_idiv(pN - pS, &P.idy);
-    uint64_t bx = kg_bits(gx), by = kg_bits(gy);
-    /* the reference's three branches (src/Kobayashi.cpp:154-167) with one
-     * shared atan call, so that lanes on different branches do not run it
-     * one after the other; theta = off + atan(gy/gx), off in {0, pi, 2 pi}
-     * (for off = 0 the atan value itself: adding +0 could turn -0 into +0) */
-    bool gx_small = kg_small(bx), gx_pos = kg_pos_big(bx), gx_neg = kg_neg_big(bx);
-    bool gy_pos = kg_pos_big(by), gy_neg = kg_neg_big(by);
-    if (gx_small) {
-        if (gy_neg)
-            theta = -0.5 * KG_PI;
-        else if (gy_pos)
-            theta = 0.5 * KG_PI;
-    }
-    bool use_atan = gx_neg || (gx_pos && (gy_pos || gy_neg));
-    if (use_atan) {
-#if KG_GDIV
-        double at = kg_atan(kg_gdiv(gy, gx));
-#else
-        double at = kg_atan(gy / gx);
+    double gx, gy;
+#if KG_QUIET
+    /* four +0 neighbours: both differences are +0 and the angle keeps its value (the dead zone) */
+    const bool quiet = (kg_bits(pE) | kg_bits(pW) | kg_bits(pN) | kg_bits(pS)) == 0;
+    if (quiet) {
+        gx = 0.0;
+        gy = 0.0;
+    } else
 #endif
-        double s = (gx_neg ? KG_PI : 2.0 * KG_PI) + at;
-        theta = (gx_neg || gy_neg) ? s : at;
+    {
+        gx = kg_idiv(pE - pW, &P.idx);
+        gy = kg_idiv(pN - pS, &P.idy);
+        uint64_t bx = kg_bits(gx), by = kg_bits(gy);
+        /* the reference's three branches (src/Kobayashi.cpp:154-167) with one
+         * shared atan call, so that lanes on different branches do not run it
+         * one after the other; theta = off + atan(gy/gx), off in {0, pi, 2 pi}
+         * (for off = 0 the atan value itself: adding +0 could turn -0 into +0) */
+        bool gx_small = kg_small(bx), gx_pos = kg_pos_big(bx), gx_neg = kg_neg_big(bx);
+        bool gy_pos = kg_pos_big(by), gy_neg = kg_neg_big(by);
+        if (gx_small) {
+            if (gy_neg)
+                theta = -0.5 * KG_PI;
+            else if (gy_pos)
+                theta = 0.5 * KG_PI;
+        }
+        bool use_atan = gx_neg || (gx_pos && (gy_pos || gy_neg));
+        if (use_atan) {
+#if KG_GDIV
+            double at = kg_atan(kg_gdiv(gy, gx));
+#else
+            double at = kg_atan(gy / gx);
+#endif
+            double s = (gx_neg ? KG_PI : 2.0 * KG_PI) + at;
+            theta = (gx_neg || gy_neg) ? s : at;
+        }
     }
     /* theta == +0 (every cell the front has not reached) gives arg0 exactly; skip the two FP64 ops */
     double arg = P.arg0;
@@ -153,8 +176,17 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
     o.gx = gx;
     o.gy = gy;
     o.e2 = e2;
-    o.a = ee * gx;
-    o.b = ee * gy;
+#if KG_QUIET
+    if (quiet && (kg_bits(ee) & KG_ABS_MASK) < KG_INF_BITS) {
+        /* ee (+0) for a finite ee: a zero with ee's sign */
+        o.a = kg_from_bits(kg_bits(ee) & ~KG_ABS_MASK);
+        o.b = o.a;
+    } else
+#endif
+    {
+        o.a = ee * gx;
+        o.b = ee * gy;
+    }
     return o;
 }
 
@@ -261,6 +293,75 @@ __device__ __forceinline__ void kg_stage2(const KgDev& P, double e2c, double gx,
     }
 }
 
+/*
+ * The phi/T update of one cell from its 3x3 phi and T neighbourhoods (rows
+ * below/at/above as pointers into shared memory, centre column k) and its
+ * neighbours' stage-1 values, with the quiet-cell shortcut:
+ *   all nine phi are +0, the neighbours' eps eps' phi_x (N, S) and
+ *   eps eps' phi_y (E, W) are zeros, grad eps^2 is flat and finite, eps^2 is
+ *   finite and T is not NaN.  Then term1, term2, eps^2 lap phi, term3 and the
+ *   double well (+0 times a finite factor) are all zeros, so the phi update
+ *   adds a zero to +0: phi stays +0.  T becomes (T + lap_T dt) + K (+0 - +0),
+ *   whose last term is the zero P.zk; with nine +0 T values it is +0.
+ * Everything else takes kg_stage2.
+ */
+__device__ __forceinline__ void kg_update_cell(const KgDev& P, const double* __restrict__ pS_, const double* __restrict__ p0,
+                                               const double* __restrict__ pN_, const double* __restrict__ tS_,
+                                               const double* __restrict__ t0, const double* __restrict__ tN_, int k,
+                                               double e2c, double gx, double gy, double e2E, double e2W, double e2N,
+                                               double e2S, double aN, double aS, double bE, double bW, double& phi,
+                                               double& t)
+{
+#define KG_LAP9(r0, rN, rS) \
+    kg_lap(P, r0[k], r0[k + 1], r0[k - 1], rN[k], rS[k], rN[k + 1], rS[k - 1], rN[k - 1], rS[k + 1])
+#define KG_OR9(r0, rN, rS)                                                                                       \
+    (kg_bits(r0[k]) | kg_bits(r0[k + 1]) | kg_bits(r0[k - 1]) | kg_bits(rN[k]) | kg_bits(rS[k]) |               \
+     kg_bits(rN[k + 1]) | kg_bits(rS[k - 1]) | kg_bits(rN[k - 1]) | kg_bits(rS[k + 1]))
+    phi = p0[k];
+    t = t0[k];
+#if KG_QUIET
+    if (KG_OR9(p0, pN_, pS_) == 0) {
+        const uint64_t ue = kg_bits(e2E), un = kg_bits(e2N);
+        const bool quiet = ((kg_bits(aN) | kg_bits(aS) | kg_bits(bE) | kg_bits(bW)) & KG_ABS_MASK) == 0 &&
+                           ue == kg_bits(e2W) && un == kg_bits(e2S) && (ue & KG_ABS_MASK) < KG_INF_BITS &&
+                           (un & KG_ABS_MASK) < KG_INF_BITS && (kg_bits(e2c) & KG_ABS_MASK) < KG_INF_BITS &&
+                           (kg_bits(t) & KG_ABS_MASK) <= KG_INF_BITS;
+        if (quiet) {
+            phi = 0.0;
+            if (KG_OR9(t0, tN_, tS_) == 0) {
+                t = 0.0;
+            } else {
+                const double x = t + KG_LAP9(t0, tN_, tS_) * P.dt;
+                const uint64_t bx = kg_bits(x);
+                if ((bx & KG_ABS_MASK) == 0)
+                    t = kg_from_bits(bx & P.zk); /* a zero plus a zero: -0 only if both are */
+                else if ((bx & KG_ABS_MASK) < KG_INF_BITS)
+                    t = x;
+                else
+                    t = x + kg_from_bits(P.zk);
+            }
+            return;
+        }
+    }
+#endif
+    const double lap_phi = KG_LAP9(p0, pN_, pS_);
+    const double lap_t = KG_LAP9(t0, tN_, tS_);
+    kg_stage2(P, e2c, gx, gy, e2E, e2W, e2N, e2S, aN, aS, bE, bW, lap_phi, lap_t, phi, t);
+#undef KG_LAP9
+#undef KG_OR9
+}
+
+/* a global load: the plain (read-only cache) path, or with COH one that stays coherent with stores
+ * other CTAs made earlier in the same kernel (L2 only) */
+template <bool COH>
+__device__ __forceinline__ double kg_ld(const double* p)
+{
+    if constexpr (COH)
+        return __ldcg(p);
+    else
+        return *p;
+}
+
 __device__ __forceinline__ int kg_wrap(int i, int n)
 {
     int r = i % n;
@@ -349,9 +450,11 @@ __device__ __forceinline__ void kg_bulk_copy(void* dst, const void* src, unsigne
  * CTA waits on that row's mbarrier; otherwise every lane loads its own
  * column (wrapped).  Ring slots are indexed by the row's position in the
  * strip, (row - (j0-2)) & 7.  `err` (may be null) receives a time-out of a
- * bulk-copy wait.
+ * bulk-copy wait.  With COH the per-lane loads bypass the SM's L1 and
+ * read-only caches (a persistent kernel reads data other CTAs wrote earlier in
+ * the same launch).
  */
-template <int NT, bool TAPE = false>
+template <int NT, bool TAPE = false, bool COH = false>
 __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const double* __restrict__ phi_in,
                                          const double* __restrict__ t_in, const double* __restrict__ th_in,
                                          double* __restrict__ phi_out, double* __restrict__ t_out,
@@ -370,9 +473,9 @@ __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const d
 
     auto load_phi_row = [&](int q) {
         const double* row = phi_in + (size_t)kg_wrap(q, ny) * nx;
-        sm.phi[(q - base) & 7][L] = row[colA];
+        sm.phi[(q - base) & 7][L] = kg_ld<COH>(row + colA);
         if (L < 2)
-            sm.phi[(q - base) & 7][NT + L] = row[colB];
+            sm.phi[(q - base) & 7][NT + L] = kg_ld<COH>(row + colB);
     };
     /* mbarriers count each ring's rows from the ring's first row (phi: j0-2, T: j0-1), so that the
      * k-th arrival at a barrier is its phase k: row q waits on phase (q - first) >> 3 */
@@ -442,9 +545,9 @@ __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const d
         } else {
             /* loads: phi row r+1, T row r */
             load_phi_row(r + 1);
-            sm.t[(r - base) & 7][L + 1] = t_in[roff + col];
+            sm.t[(r - base) & 7][L + 1] = kg_ld<COH>(t_in + roff + col);
         }
-        double theta = th_in[roff + col];
+        double theta = kg_ld<COH>(th_in + roff + col);
         /* the row barrier, which also makes a bulk-copy time-out a CTA-wide decision (a one-warp
          * strip, NT = 32, needs only a warp vote: warps never wait on each other) */
         bool fail;
@@ -478,15 +581,16 @@ __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const d
         if (out_lane && s >= j0) {
             const int sm1 = (s - 1 - base) & 7, s0 = (s - base) & 7, sp1 = (s + 1 - base) & 7;
             const int k = L + 1;
-            double lap_phi = kg_lap(P, sm.phi[s0][k], sm.phi[s0][k + 1], sm.phi[s0][k - 1], sm.phi[sp1][k],
-                                    sm.phi[sm1][k], sm.phi[sp1][k + 1], sm.phi[sm1][k - 1], sm.phi[sp1][k - 1],
-                                    sm.phi[sm1][k + 1]);
-            double lap_t = kg_lap(P, sm.t[s0][k], sm.t[s0][k + 1], sm.t[s0][k - 1], sm.t[sp1][k], sm.t[sm1][k],
-                                  sm.t[sp1][k + 1], sm.t[sm1][k - 1], sm.t[sp1][k - 1], sm.t[sm1][k + 1]);
-            double phi = sm.phi[s0][k];
-            double t = sm.t[s0][k];
             const size_t soff = (size_t)kg_wrap(s, ny) * nx;
+            double phi, t;
             if constexpr (TAPE) {
+                double lap_phi = kg_lap(P, sm.phi[s0][k], sm.phi[s0][k + 1], sm.phi[s0][k - 1], sm.phi[sp1][k],
+                                        sm.phi[sm1][k], sm.phi[sp1][k + 1], sm.phi[sm1][k - 1], sm.phi[sp1][k - 1],
+                                        sm.phi[sm1][k + 1]);
+                double lap_t = kg_lap(P, sm.t[s0][k], sm.t[s0][k + 1], sm.t[s0][k - 1], sm.t[sp1][k], sm.t[sm1][k],
+                                      sm.t[sp1][k + 1], sm.t[sm1][k - 1], sm.t[sp1][k - 1], sm.t[sm1][k + 1]);
+                phi = sm.phi[s0][k];
+                t = sm.t[s0][k];
                 KgS2Aux aux;
                 tape->f[KG_TAPE_PHI][soff + col] = phi;
                 tape->f[KG_TAPE_T][soff + col] = t;
@@ -498,8 +602,9 @@ __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const d
                 tape->f[KG_TAPE_GEX][soff + col] = aux.gex;
                 tape->f[KG_TAPE_GEY][soff + col] = aux.gey;
             } else {
-                kg_stage2(P, e2_m1, gx_m1, gy_m1, sm.e2[s & 1][L + 1], sm.e2[s & 1][L - 1], s1.e2, e2_m2, s1.a, a_m2,
-                          sm.b[s & 1][L + 1], sm.b[s & 1][L - 1], lap_phi, lap_t, phi, t);
+                kg_update_cell(P, sm.phi[sm1], sm.phi[s0], sm.phi[sp1], sm.t[sm1], sm.t[s0], sm.t[sp1], k, e2_m1, gx_m1,
+                               gy_m1, sm.e2[s & 1][L + 1], sm.e2[s & 1][L - 1], s1.e2, e2_m2, s1.a, a_m2,
+                               sm.b[s & 1][L + 1], sm.b[s & 1][L - 1], phi, t);
             }
             phi_out[soff + col] = phi;
             t_out[soff + col] = t;
@@ -521,5 +626,138 @@ __device__ __forceinline__ void kg_strip(const KgDev& P, int nx, int ny, const d
             kg_mbar_wait(phi_bar(q), phi_par(q), nullptr);
         for (int q = max(j0 - 1, last_t - 7); q <= last_t; q++)
             kg_mbar_wait(t_bar(q), t_par(q), nullptr);
+    }
+}
+
+/*
+ * Temporal blocking, k = 2: one CTA of NT threads advances columns
+ * [i0, i0+NT-6) and rows [j0, j0+bh) (clipped to the grid) by TWO steps in one
+ * pass over HBM.  Two marching pipelines share the row loop:
+ *   pipeline 1 is the k = 1 strip on columns i0-3 .. i0+NT-4 (lane L <->
+ *   column i0-3+L): at row r it runs stage 1 of step 1, and stage 2 of step 1
+ *   for row r-1 on lanes 1..NT-2; the step-1 phi and T of that row go to
+ *   shared-memory rings (phi1, t1) instead of HBM, and the step-1 theta of
+ *   each lane's column waits two rows in registers;
+ *   pipeline 2 runs stage 1 of step 2 for row r-2 (lanes 1..NT-2) from those
+ *   rings, and stage 2 of step 2 for row r-3 on the output lanes 3..NT-4.
+ * The halo is therefore 4 columns and 3 rows on each side for phi (2 per
+ * step), and every cell of the intermediate step is computed with exactly the
+ * operations of the k = 1 step, so results are bit-identical to two k = 1
+ * steps.  One __syncthreads per row serves both pipelines: within a row's
+ * compute no lane reads a ring slot or exchange slot another lane writes in
+ * the same row, and the next row's loads only refill slots no longer read.
+ * Shared memory: 41 KB at NT = 128.
+ */
+template <int NT>
+struct __align__(16) KgSmem2 {
+    double phi[8][NT + 2]; /* step-0 phi: column i0-4+k at [.][k]; row q at slot (q - (j0-4)) & 7 */
+    double t[8][NT + 2];   /* step-0 T, same layout */
+    double e2a[2][NT];     /* step-1 eps^2 and eps eps' phi_y of lane L at [row & 1][L] */
+    double ba[2][NT];
+    double phi1[8][NT];    /* step-1 phi of lane L's column at [slot][L] */
+    double t1[8][NT];
+    double e2b[2][NT];     /* step-2 exchange, as e2a/ba */
+    double bb[2][NT];
+};
+
+template <int NT, bool COH = false>
+__device__ __forceinline__ void kg_strip2(const KgDev& P, int nx, int ny, const double* __restrict__ phi_in,
+                                          const double* __restrict__ t_in, const double* __restrict__ th_in,
+                                          double* __restrict__ phi_out, double* __restrict__ t_out,
+                                          double* __restrict__ th_out, int i0, int j0, int bh, KgSmem2<NT>& sm)
+{
+    static_assert(NT >= 8, "temporal blocking needs at least 8 lanes");
+    const int L = threadIdx.x;
+    const int jend = min(j0 + bh, ny);
+    const int base = j0 - 4; /* row of ring slot 0 */
+    const int colA = kg_wrap(i0 - 4 + L, nx);
+    const int colB = (L < 2) ? kg_wrap(i0 - 4 + NT + L, nx) : 0;
+    const int col = kg_wrap(i0 - 3 + L, nx);
+    const bool lane1 = (L >= 1) && (L <= NT - 2);                                    /* step-1 stage 2, step-2 stage 1 */
+    const bool out_lane = (L >= 3) && (L <= NT - 4) && (i0 - 3 + L < nx);           /* step-2 stage 2, outputs */
+    auto load_phi_row = [&](int q) {
+        const double* row = phi_in + (size_t)kg_wrap(q, ny) * nx;
+        sm.phi[(q - base) & 7][L] = kg_ld<COH>(row + colA);
+        if (L < 2)
+            sm.phi[(q - base) & 7][NT + L] = kg_ld<COH>(row + colB);
+    };
+    load_phi_row(j0 - 4);
+    load_phi_row(j0 - 3);
+
+    /* pipeline 1 window (stage-1 results of rows r-2, r-1), pipeline 2 window, step-1 theta queue */
+    double e2a_m2 = 0, aa_m2 = 0, e2a_m1 = 0, aa_m1 = 0, gxa_m1 = 0, gya_m1 = 0;
+    double e2b_m2 = 0, ab_m2 = 0, e2b_m1 = 0, ab_m1 = 0, gxb_m1 = 0, gyb_m1 = 0;
+    double th1_m1 = 0, th1_m2 = 0;
+    for (int r = j0 - 3; r <= jend + 2; r++) {
+        const size_t roff = (size_t)kg_wrap(r, ny) * nx;
+        load_phi_row(r + 1);
+        sm.t[(r - base) & 7][L + 1] = kg_ld<COH>(t_in + roff + col);
+        double theta = kg_ld<COH>(th_in + roff + col);
+        if constexpr (NT == 32)
+            __syncwarp();
+        else
+            __syncthreads();
+
+        /* ---- step 1: stage 1 at row r (all lanes) ---- */
+        const int rm = (r - 1 - base) & 7, r0 = (r - base) & 7, rp = (r + 1 - base) & 7;
+        KgS1 sa = kg_stage1(P, sm.phi[r0][L + 2], sm.phi[r0][L], sm.phi[rp][L + 1], sm.phi[rm][L + 1], theta);
+        sm.e2a[r & 1][L] = sa.e2;
+        sm.ba[r & 1][L] = sa.b;
+        /* ---- step 1: stage 2 at row s = r-1 -> phi1, t1 ---- */
+        const int s = r - 1;
+        if (s >= j0 - 2) {
+            const int ss = (s - base) & 7;
+            double phi = 0.0, t = 0.0;
+            if (lane1) {
+                const int sm1 = (s - 1 - base) & 7, sp1 = (s + 1 - base) & 7;
+                kg_update_cell(P, sm.phi[sm1], sm.phi[ss], sm.phi[sp1], sm.t[sm1], sm.t[ss], sm.t[sp1], L + 1, e2a_m1,
+                               gxa_m1, gya_m1, sm.e2a[s & 1][L + 1], sm.e2a[s & 1][L - 1], sa.e2, e2a_m2, sa.a, aa_m2,
+                               sm.ba[s & 1][L + 1], sm.ba[s & 1][L - 1], phi, t);
+            }
+            sm.phi1[ss][L] = phi;
+            sm.t1[ss][L] = t;
+        }
+        e2a_m2 = e2a_m1;
+        aa_m2 = aa_m1;
+        e2a_m1 = sa.e2;
+        aa_m1 = sa.a;
+        gxa_m1 = sa.gx;
+        gya_m1 = sa.gy;
+        /* step-1 theta of row r-2 for this lane's column */
+        double th1 = th1_m2;
+        th1_m2 = th1_m1;
+        th1_m1 = theta;
+
+        /* ---- step 2: stage 1 at row q = r-2 from the step-1 rings ---- */
+        const int q = r - 2;
+        if (q >= j0 - 1) {
+            const int qm = (q - 1 - base) & 7, q0 = (q - base) & 7, qp = (q + 1 - base) & 7;
+            KgS1 sb{};
+            if (lane1) {
+                sb = kg_stage1(P, sm.phi1[q0][L + 1], sm.phi1[q0][L - 1], sm.phi1[qp][L], sm.phi1[qm][L], th1);
+                sm.e2b[q & 1][L] = sb.e2;
+                sm.bb[q & 1][L] = sb.b;
+                if (out_lane && q >= j0 && q < jend)
+                    th_out[(size_t)kg_wrap(q, ny) * nx + col] = th1;
+            }
+            /* ---- step 2: stage 2 at row u = r-3 -> outputs ---- */
+            const int u = r - 3;
+            if (out_lane && u >= j0 && u < jend) {
+                const int um = (u - 1 - base) & 7, u0 = (u - base) & 7, up = (u + 1 - base) & 7;
+                double phi, t;
+                kg_update_cell(P, sm.phi1[um], sm.phi1[u0], sm.phi1[up], sm.t1[um], sm.t1[u0], sm.t1[up], L, e2b_m1,
+                               gxb_m1, gyb_m1, sm.e2b[u & 1][L + 1], sm.e2b[u & 1][L - 1], sb.e2, e2b_m2, sb.a, ab_m2,
+                               sm.bb[u & 1][L + 1], sm.bb[u & 1][L - 1], phi, t);
+                const size_t uoff = (size_t)kg_wrap(u, ny) * nx;
+                phi_out[uoff + col] = phi;
+                t_out[uoff + col] = t;
+            }
+            e2b_m2 = e2b_m1;
+            ab_m2 = ab_m1;
+            e2b_m1 = sb.e2;
+            ab_m1 = sb.a;
+            gxb_m1 = sb.gx;
+            gyb_m1 = sb.gy;
+        }
     }
 }

@@ -3,6 +3,7 @@
  * host-vs-device tests, and an FP64 FMA throughput probe.
  */
 #include "kg_common.h"
+#include <stdlib.h>
 #include <string.h>
 #include "kobayashi_diag.h"
 
@@ -72,58 +73,178 @@ extern "C" int kg_diag_eval(int fn, const double* x, double* y, long long n, dou
     return KG_OK;
 }
 
-#define KG_PEAK_CHAINS 8
+/*
+ * FP64 pipe probe.  Every thread runs CHAINS independent dependency chains of
+ * one FP64 operation (OP 0: FMA, 1: add, 2: multiply, 3: two adds and one
+ * multiply, the step's own mix), KG_PEAK_ITERS times.  Thread 0 of each CTA
+ * records its SM and the SM clock at its start and end, so the rate per SM
+ * clock comes out without knowing the clock frequency.
+ */
 #define KG_PEAK_ITERS 4096
 
-__global__ void kg_diag_fma_kernel(double* out, double s)
+template <int OP, int CHAINS>
+__global__ void kg_diag_fp64_kernel(double* out, double s, long long* stamps)
 {
-    double v[KG_PEAK_CHAINS];
-    for (int c = 0; c < KG_PEAK_CHAINS; c++)
+    long long t0 = clock64();
+    double v[CHAINS];
+#pragma unroll
+    for (int c = 0; c < CHAINS; c++)
         v[c] = 1.0 + 1e-3 * (threadIdx.x + c);
     for (int i = 0; i < KG_PEAK_ITERS; i++) {
 #pragma unroll
-        for (int c = 0; c < KG_PEAK_CHAINS; c++)
-            v[c] = __fma_rn(v[c], s, 0.5);
+        for (int c = 0; c < CHAINS; c++) {
+            if constexpr (OP == 0)
+                v[c] = __fma_rn(v[c], s, 0.5);
+            else if constexpr (OP == 1)
+                v[c] = __dadd_rn(v[c], s);
+            else if constexpr (OP == 2)
+                v[c] = __dmul_rn(v[c], s);
+            else
+                v[c] = (c % 3 == 2) ? __dmul_rn(v[c], s) : __dadd_rn(v[c], s);
+        }
     }
     double acc = 0;
-    for (int c = 0; c < KG_PEAK_CHAINS; c++)
+#pragma unroll
+    for (int c = 0; c < CHAINS; c++)
         acc += v[c];
     if (acc == 12345.678)
         out[0] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        stamps[3 * blockIdx.x] = smid;
+        stamps[3 * blockIdx.x + 1] = t0;
+        stamps[3 * blockIdx.x + 2] = clock64();
+    }
 }
 
+typedef void (*kg_fp64_kernel_t)(double*, double, long long*);
+
+static kg_fp64_kernel_t fp64_kernel(int op, int chains)
+{
+#define KG_K(o)                                                                       \
+    (chains == 4 ? kg_diag_fp64_kernel<o, 4> : chains == 8 ? kg_diag_fp64_kernel<o, 8> \
+                                                            : kg_diag_fp64_kernel<o, 16>)
+    switch (op) {
+    case 0: return KG_K(0);
+    case 1: return KG_K(1);
+    case 2: return KG_K(2);
+    default: return KG_K(3);
+    }
+#undef KG_K
+}
+
+extern "C" int kg_diag_fp64_probe(int op, int chains, int ctas_per_sm, int threads, double* lanes_per_s,
+                                  double* lanes_per_sm_clock)
+{
+    if (op < 0 || op > 3 || (chains != 4 && chains != 8 && chains != 16) || ctas_per_sm < 1 || ctas_per_sm > 16 ||
+        (threads != 64 && threads != 128 && threads != 256 && threads != 512) || !lanes_per_s)
+        return kg_fail(KG_ERR_INVALID, "kg_diag_fp64_probe: bad arguments");
+    int dev = 0, sms = 0;
+    KG_CUDA(cudaGetDevice(&dev));
+    KG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * ctas_per_sm;
+    kg_fp64_kernel_t k = fp64_kernel(op, chains);
+    int fit = 0;
+    KG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k, threads, 0));
+    if (fit < ctas_per_sm)
+        return kg_fail(KG_ERR_INVALID, "kg_diag_fp64_probe: only %d CTAs of %d threads fit on an SM", fit, threads);
+    double* out = nullptr;
+    long long* stamps = nullptr;
+    KG_CUDA(cudaMalloc(&out, sizeof(double)));
+    cudaError_t e = cudaMalloc(&stamps, sizeof(long long) * 3 * blocks);
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&a);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&b);
+    float best = 1e30f;
+    double best_clk = 0;
+    long long* h = (long long*)malloc(sizeof(long long) * 3 * blocks);
+    double* sm_lo = (double*)malloc(sizeof(double) * 3 * sms); /* per SM: first start, last end, CTAs */
+    if (!h || !sm_lo)
+        e = cudaErrorMemoryAllocation;
+    for (int r = 0; r < 4 && e == cudaSuccess; r++) {
+        cudaEventRecord(a);
+        k<<<blocks, threads>>>(out, 0.999, stamps);
+        cudaEventRecord(b);
+        e = cudaEventSynchronize(b);
+        if (e == cudaSuccess)
+            e = cudaGetLastError();
+        if (e != cudaSuccess || r == 0)
+            continue; /* the first launch warms up */
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        e = cudaMemcpy(h, stamps, sizeof(long long) * 3 * blocks, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess)
+            break;
+        /* per SM: the lanes its CTAs ran between the first start and the last end (clock64 counts that
+         * SM's own clock) */
+        for (int i = 0; i < sms; i++) {
+            sm_lo[3 * i] = 1e300;
+            sm_lo[3 * i + 1] = -1e300;
+            sm_lo[3 * i + 2] = 0;
+        }
+        for (int i = 0; i < blocks; i++) {
+            int id = (int)h[3 * i];
+            if (id < 0 || id >= sms)
+                continue;
+            if ((double)h[3 * i + 1] < sm_lo[3 * id])
+                sm_lo[3 * id] = (double)h[3 * i + 1];
+            if ((double)h[3 * i + 2] > sm_lo[3 * id + 1])
+                sm_lo[3 * id + 1] = (double)h[3 * i + 2];
+            sm_lo[3 * id + 2] += 1;
+        }
+        double rate = 0;
+        int used = 0;
+        const double lanes_per_cta = (double)threads * KG_PEAK_ITERS * chains;
+        for (int i = 0; i < sms; i++)
+            if (sm_lo[3 * i + 1] > sm_lo[3 * i]) {
+                used++;
+                rate += sm_lo[3 * i + 2] * lanes_per_cta / (sm_lo[3 * i + 1] - sm_lo[3 * i]);
+            }
+        if (ms < best) {
+            best = ms;
+            best_clk = used ? rate / used : 0;
+        }
+    }
+    free(h);
+    free(sm_lo);
+    if (a)
+        cudaEventDestroy(a);
+    if (b)
+        cudaEventDestroy(b);
+    cudaFree(out);
+    cudaFree(stamps);
+    if (e != cudaSuccess)
+        return kg_cuda_fail(e, "kg_diag_fp64_probe");
+    *lanes_per_s = (double)blocks * threads * KG_PEAK_ITERS * chains / (best * 1e-3);
+    if (lanes_per_sm_clock)
+        *lanes_per_sm_clock = best_clk;
+    return KG_OK;
+}
+
+/* the best FP64 lane rate over a sweep of operations, chain counts and CTAs per SM */
 extern "C" int kg_diag_fp64_peak(double* ops_per_s)
 {
     if (!ops_per_s)
         return kg_fail(KG_ERR_INVALID, "kg_diag_fp64_peak: null pointer");
-    int dev = 0, sms = 0;
-    KG_CUDA(cudaGetDevice(&dev));
-    KG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    double* out = nullptr;
-    KG_CUDA(cudaMalloc(&out, sizeof(double)));
-    cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
-    const int blocks = sms * 4, threads = 256;
-    kg_diag_fma_kernel<<<blocks, threads>>>(out, 0.999);
-    float best = 1e30f;
-    for (int r = 0; r < 3; r++) {
-        cudaEventRecord(a);
-        kg_diag_fma_kernel<<<blocks, threads>>>(out, 0.999);
-        cudaEventRecord(b);
-        cudaEventSynchronize(b);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, a, b);
-        if (ms < best)
-            best = ms;
-    }
-    cudaError_t e = cudaGetLastError();
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    cudaFree(out);
-    if (e != cudaSuccess)
-        return kg_cuda_fail(e, "kg_diag_fp64_peak");
-    *ops_per_s = (double)blocks * threads * KG_PEAK_ITERS * KG_PEAK_CHAINS / (best * 1e-3);
+    double best = 0;
+    const int ctas[3] = {2, 4, 8};
+    for (int op = 0; op < 4; op++)
+        for (int chains : {8, 16})
+            for (int c : ctas) {
+                double v = 0;
+                int rc = kg_diag_fp64_probe(op, chains, c, 256, &v, nullptr);
+                if (rc == KG_ERR_INVALID)
+                    continue; /* that many CTAs do not fit */
+                if (rc)
+                    return rc;
+                if (v > best)
+                    best = v;
+            }
+    *ops_per_s = best;
     return KG_OK;
 }
 

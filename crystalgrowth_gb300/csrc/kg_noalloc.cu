@@ -15,6 +15,10 @@
  * Limit: grids of at most KG_NOALLOC_MAX_CELLS cells (512 x 512).  The array
  * (3 fields x 2^18 cells x 8 bytes = 6 MiB) is part of the library's device
  * image, so every GPU that loads the library holds it until the process exits.
+ *
+ * The step is the same fused strip as kg_step's, with per-lane row loads only
+ * (no bulk copies, so it has no bounded wait that could time out) and a fixed
+ * strip shape: results are identical to kg_step's, speed may differ.
  */
 #include <mutex>
 #include "kg_common.h"
@@ -40,7 +44,9 @@ __global__ void __launch_bounds__(NT) kg_noalloc_step_kernel(const __grid_consta
 /* Device address of the scratch array on the current device.  Host code
  * cannot use kg_noalloc_scratch directly: on the host that name only stands
  * for the symbol.  The address is looked up once per device, with that device
- * current, and kept. */
+ * current, and kept; the same first call also makes the runtime load the step
+ * kernel (with lazy module loading it would otherwise load at its first
+ * launch), so a first call with nsteps = 0 prepares the device completely. */
 static int noalloc_scratch(double** out)
 {
     static std::mutex mu;
@@ -55,6 +61,10 @@ static int noalloc_scratch(double** out)
         cudaError_t e = cudaGetSymbolAddress(&p, kg_noalloc_scratch);
         if (e != cudaSuccess)
             return kg_cuda_fail(e, "kg_step_noalloc: cudaGetSymbolAddress of the scratch array");
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, kg_noalloc_step_kernel<128>);
+        if (e != cudaSuccess)
+            return kg_cuda_fail(e, "kg_step_noalloc: loading the step kernel");
         addr[dev] = (double*)p;
     }
     *out = addr[dev];

@@ -6,12 +6,14 @@
  * (src/Kobayashi.h:107-115).  kg_step launches one fused kernel per time step
  * (kg_device.cuh) and replays them as CUDA graphs of `chunk` steps.
  */
+#include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <new>
 #include "kg_common.h"
 #include "kobayashi_color.h"
+#include "kobayashi_diag.h"
 
 
 /* resident CTAs per SM the register allocation must allow (0: the compiler's choice) */
@@ -45,6 +47,18 @@ __global__ void KG_STEP_BOUNDS(NT) kg_step_kernel(const __grid_constant__ KgDev 
                  err);
 }
 
+/* two steps per launch (temporal blocking, k = 2); per-lane loads only */
+template <int NT>
+__global__ void KG_STEP_BOUNDS(NT) kg_step2_kernel(const __grid_constant__ KgDev P, int nx, int ny, int bh,
+                                                      const double* __restrict__ phi_in, const double* __restrict__ t_in,
+                                                      const double* __restrict__ th_in, double* __restrict__ phi_out,
+                                                      double* __restrict__ t_out, double* __restrict__ th_out)
+{
+    __shared__ KgSmem2<NT> sm;
+    kg_strip2<NT>(P, nx, ny, phi_in, t_in, th_in, phi_out, t_out, th_out, blockIdx.x * (NT - 6), blockIdx.y * bh, bh,
+                  sm);
+}
+
 struct kg_sim {
     int nx = 0, ny = 0;
     kg_params p{};
@@ -57,12 +71,22 @@ struct kg_sim {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int nt = 128; /* threads per strip CTA (strip width nt - 2 columns) */
     int bh = 64;  /* rows per strip */
+    int tblock = 1; /* time steps per launch: 1, or 2 (temporal blocking) */
     float* color = nullptr; /* RGBA staging buffer for kg_colormap, allocated on first use */
     unsigned* err = nullptr; /* raised by a kernel whose bounded wait ran out */
+    /* set once a bounded wait ran out: the state is unreliable, and kg_step refuses until the state
+     * is replaced (kg_reset, kg_seed_disks, kg_set_fields with all three fields, kg_load) */
+    bool failed = false;
 };
 
+/* Destroys the instantiated graphs.  A graph launched earlier may still be running on the
+ * handle's stream, so the stream is drained first. */
 static void drop_graphs(kg_sim* h)
 {
+    if (!h->graph[0] && !h->graph[1])
+        return;
+    if (h->stream)
+        cudaStreamSynchronize(h->stream);
     for (int k = 0; k < 2; k++)
         if (h->graph[k]) {
             cudaGraphExecDestroy(h->graph[k]);
@@ -70,23 +94,55 @@ static void drop_graphs(kg_sim* h)
         }
 }
 
-static int launch_step(kg_sim* h, int from)
+/* one launch advancing `k` (1 or 2) steps from ping-pong copy `from` into copy from ^ 1 */
+static int launch_step(kg_sim* h, int from, int k = 1)
 {
-    dim3 grid((h->nx + h->nt - 3) / (h->nt - 2), (h->ny + h->bh - 1) / h->bh);
     double* const* a = h->buf[from];
     double* const* b = h->buf[from ^ 1];
-    if (h->nt == 32)
-        kg_step_kernel<32><<<grid, 32, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1], b[2],
-                                                        h->err);
-    else if (h->nt == 64)
-        kg_step_kernel<64><<<grid, 64, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1], b[2],
-                                                        h->err);
-    else
-        kg_step_kernel<128><<<grid, 128, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1],
-                                                          b[2], h->err);
+    if (k == 2) {
+        dim3 grid((h->nx + h->nt - 7) / (h->nt - 6), (h->ny + h->bh - 1) / h->bh);
+        if (h->nt == 32)
+            kg_step2_kernel<32><<<grid, 32, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1],
+                                                             b[2]);
+        else if (h->nt == 64)
+            kg_step2_kernel<64><<<grid, 64, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1],
+                                                             b[2]);
+        else
+            kg_step2_kernel<128><<<grid, 128, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0],
+                                                               b[1], b[2]);
+    } else {
+        dim3 grid((h->nx + h->nt - 3) / (h->nt - 2), (h->ny + h->bh - 1) / h->bh);
+        if (h->nt == 32)
+            kg_step_kernel<32><<<grid, 32, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1],
+                                                            b[2], h->err);
+        else if (h->nt == 64)
+            kg_step_kernel<64><<<grid, 64, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1],
+                                                            b[2], h->err);
+        else
+            kg_step_kernel<128><<<grid, 128, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0],
+                                                              b[1], b[2], h->err);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
-        return kg_cuda_fail(e, "kg_step_kernel launch");
+        return kg_cuda_fail(e, k == 2 ? "kg_step2_kernel launch" : "kg_step_kernel launch");
+    return KG_OK;
+}
+
+/* launches that advance n steps with the handle's temporal blocking factor */
+static long long launches_for(const kg_sim* h, long long n) { return h->tblock == 2 ? n / 2 + (n & 1) : n; }
+
+/* enqueues n steps from copy `from`; the result lies in copy from ^ (launches_for(n) & 1) */
+static int enqueue_steps(kg_sim* h, int from, long long n)
+{
+    int c = from;
+    for (long long s = 0; s < n;) {
+        const int k = (h->tblock == 2 && n - s >= 2) ? 2 : 1;
+        int rc = launch_step(h, c, k);
+        if (rc)
+            return rc;
+        c ^= 1;
+        s += k;
+    }
     return KG_OK;
 }
 
@@ -95,12 +151,7 @@ static int build_graph(kg_sim* h, int from)
 {
     cudaGraph_t g = nullptr;
     KG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = KG_OK;
-    int c = from;
-    for (int s = 0; s < h->chunk && rc == KG_OK; s++) {
-        rc = launch_step(h, c);
-        c ^= 1;
-    }
+    int rc = enqueue_steps(h, from, h->chunk);
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     if (rc != KG_OK) {
         if (g)
@@ -129,9 +180,9 @@ extern "C" int kg_destroy(kg_sim* h)
 {
     if (!h)
         return KG_OK;
-    drop_graphs(h);
     if (h->stream)
         cudaStreamSynchronize(h->stream);
+    drop_graphs(h);
     for (int k = 0; k < 2; k++)
         for (int f = 0; f < 3; f++)
             if (h->buf[k][f])
@@ -155,6 +206,7 @@ extern "C" int kg_seed_disks(kg_sim* h, int n, const int* cx, const int* cy, con
     rc = kg_seed_device(a[0], a[1], a[2], h->nx, h->ny, n, cx, cy, r, h->stream);
     if (rc)
         return rc;
+    h->failed = false;
     h->steps = 0;
     h->frames = 0;
     return KG_OK;
@@ -266,6 +318,29 @@ extern "C" int kg_set_tile(kg_sim* h, int nt, int bh)
     return KG_OK;
 }
 
+extern "C" int kg_set_tblock(kg_sim* h, int k)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (k != 1 && k != 2)
+        return kg_fail(KG_ERR_INVALID, "kg_set_tblock: the temporal blocking factor must be 1 or 2");
+    h->tblock = k;
+    drop_graphs(h);
+    return KG_OK;
+}
+
+extern "C" int kg_get_tblock(const kg_sim* h, int* k)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    if (!k)
+        return kg_fail(KG_ERR_INVALID, "kg_get_tblock: null pointer");
+    *k = h->tblock;
+    return KG_OK;
+}
+
 extern "C" int kg_get_tile(const kg_sim* h, int* nt, int* bh)
 {
     int rc = check(h);
@@ -285,6 +360,9 @@ extern "C" int kg_step(kg_sim* h, long long nsteps)
         return rc;
     if (nsteps < 0)
         return kg_fail(KG_ERR_INVALID, "kg_step: negative step count");
+    if (h->failed)
+        return kg_fail(KG_ERR_TIMEOUT, "kg_step: an earlier step's bounded wait ran out and the state is "
+                                       "unreliable; replace it first (kg_reset, kg_seed_disks, kg_set_fields, kg_load)");
     while (h->chunk > 0 && nsteps >= h->chunk) {
         if (!h->graph[h->cur]) {
             rc = build_graph(h, h->cur);
@@ -294,16 +372,16 @@ extern "C" int kg_step(kg_sim* h, long long nsteps)
         cudaError_t e = cudaGraphLaunch(h->graph[h->cur], h->stream);
         if (e != cudaSuccess)
             return kg_cuda_fail(e, "cudaGraphLaunch");
-        h->cur ^= (h->chunk & 1);
+        h->cur ^= (int)(launches_for(h, h->chunk) & 1);
         h->steps += h->chunk;
         nsteps -= h->chunk;
     }
-    for (; nsteps > 0; nsteps--) {
-        rc = launch_step(h, h->cur);
+    if (nsteps > 0) {
+        rc = enqueue_steps(h, h->cur, nsteps);
         if (rc)
             return rc;
-        h->cur ^= 1;
-        h->steps++;
+        h->cur ^= (int)(launches_for(h, nsteps) & 1);
+        h->steps += nsteps;
     }
     return KG_OK;
 }
@@ -326,8 +404,25 @@ static int sync_and_check(kg_sim* h)
     if (flag) {
         cudaMemsetAsync(h->err, 0, sizeof(unsigned), h->stream);
         cudaStreamSynchronize(h->stream);
+        h->failed = true;
         return kg_fail(KG_ERR_TIMEOUT, "kg_step: a bulk-copy wait in the step kernel ran out; the state is unreliable");
     }
+    if (h->failed)
+        return kg_fail(KG_ERR_TIMEOUT, "the state is unreliable after a bounded wait ran out; replace it first "
+                                       "(kg_reset, kg_seed_disks, kg_set_fields, kg_load)");
+    return KG_OK;
+}
+
+/* Host-side fault injection for tests: raises the handle's device error flag as a kernel whose bounded
+ * wait ran out would (no kernel runs, nothing faults). */
+extern "C" int kg_diag_inject_timeout(kg_sim* h)
+{
+    int rc = check(h);
+    if (rc)
+        return rc;
+    const unsigned one = 1;
+    KG_CUDA(cudaMemcpyAsync(h->err, &one, sizeof one, cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(cudaStreamSynchronize(h->stream));
     return KG_OK;
 }
 
@@ -363,6 +458,8 @@ extern "C" int kg_set_fields(kg_sim* h, const double* phi, const double* T, cons
         if (src[f])
             KG_CUDA(cudaMemcpyAsync(h->buf[h->cur][f], src[f], bytes, cudaMemcpyHostToDevice, h->stream));
     KG_CUDA(cudaStreamSynchronize(h->stream));
+    if (phi && T && theta)
+        h->failed = false; /* the whole state was replaced */
     return KG_OK;
 }
 
@@ -447,8 +544,24 @@ extern "C" int kg_colormap(kg_sim* h, int order, float* rgba)
 
 #define KG_SNAP_HEADER 4096
 
-static const char* kg_param_names[13] = {"dx", "dy", "dt", "tau", "eps_bar", "mu", "K",
-                                          "delta", "aniso", "alpha", "gamma", "teq", "theta0"};
+/* the snapshot header's parameter keys and the kg_params member each one stores */
+static const struct {
+    const char* name;
+    size_t off;
+} kg_param_fields[] = {
+    {"dx", offsetof(kg_params, dx)},         {"dy", offsetof(kg_params, dy)},
+    {"dt", offsetof(kg_params, dt)},         {"tau", offsetof(kg_params, tau)},
+    {"eps_bar", offsetof(kg_params, eps_bar)}, {"mu", offsetof(kg_params, mu)},
+    {"K", offsetof(kg_params, K)},           {"delta", offsetof(kg_params, delta)},
+    {"aniso", offsetof(kg_params, aniso)},   {"alpha", offsetof(kg_params, alpha)},
+    {"gamma", offsetof(kg_params, gamma)},   {"teq", offsetof(kg_params, teq)},
+    {"theta0", offsetof(kg_params, theta0)},
+};
+static const int kg_nparams = (int)(sizeof kg_param_fields / sizeof kg_param_fields[0]);
+static_assert(sizeof(kg_params) == sizeof kg_param_fields / sizeof kg_param_fields[0] * sizeof(double),
+              "every kg_params member must have a snapshot key");
+
+static double* param_at(kg_params* p, int k) { return (double*)((char*)p + kg_param_fields[k].off); }
 
 extern "C" int kg_save(kg_sim* h, const char* path)
 {
@@ -464,9 +577,10 @@ extern "C" int kg_save(kg_sim* h, const char* path)
                      "\"steps\": %lld, \"frames\": %lld, \"dtype\": \"float64\", \"byteorder\": \"little\", "
                      "\"fields\": [\"phi\", \"T\", \"theta\"], \"header_bytes\": %d, \"params\": {",
                      h->nx, h->ny, h->steps, h->frames, KG_SNAP_HEADER);
-    const double* pv = &h->p.dx;
-    for (int k = 0; k < 13; k++)
-        n += snprintf(hdr + n, sizeof hdr - n, "%s\"%s\": %.17g", k ? ", " : "", kg_param_names[k], pv[k]);
+    kg_params pc = h->p;
+    for (int k = 0; k < kg_nparams; k++)
+        n += snprintf(hdr + n, sizeof hdr - n, "%s\"%s\": %.17g", k ? ", " : "", kg_param_fields[k].name,
+                      *param_at(&pc, k));
     n += snprintf(hdr + n, sizeof hdr - n, "}}");
     if (n >= KG_SNAP_HEADER - 1)
         return kg_fail(KG_ERR_INVALID, "kg_save: header overflow");
@@ -543,11 +657,11 @@ extern "C" int kg_load(kg_sim* h, const char* path)
         return kg_fail(KG_ERR_INVALID, "kg_load: snapshot is %lld x %lld, the handle is %d x %d", nx, ny, h->nx, h->ny);
     }
     kg_params p;
-    double* pv = &p.dx;
-    for (int k = 0; k < 13; k++)
-        if (snap_double(hdr, kg_param_names[k], &pv[k])) {
+    memset(&p, 0, sizeof p);
+    for (int k = 0; k < kg_nparams; k++)
+        if (snap_double(hdr, kg_param_fields[k].name, param_at(&p, k))) {
             fclose(f);
-            return kg_fail(KG_ERR_INVALID, "kg_load: parameter %s missing", kg_param_names[k]);
+            return kg_fail(KG_ERR_INVALID, "kg_load: parameter %s missing", kg_param_fields[k].name);
         }
     KgDev dev;
     rc = kg_prepare(&p, &dev);
@@ -588,6 +702,7 @@ extern "C" int kg_load(kg_sim* h, const char* path)
     h->dev = dev;
     h->steps = steps;
     h->frames = frames;
+    h->failed = false;
     drop_graphs(h);
     return KG_OK;
 }

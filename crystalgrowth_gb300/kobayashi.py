@@ -116,6 +116,15 @@ class Kobayashi:
     def set_tile(self, nt, bh):
         check(lib().kg_set_tile(self._h, int(nt), int(bh)))
 
+    def set_tblock(self, k):
+        """time steps per pass over HBM: 1, or 2 (temporal blocking; identical results)"""
+        check(lib().kg_set_tblock(self._h, int(k)))
+
+    def tblock(self):
+        k = ctypes.c_int()
+        check(lib().kg_get_tblock(self._h, ctypes.byref(k)))
+        return k.value
+
     def tile(self):
         nt, bh = ctypes.c_int(), ctypes.c_int()
         check(lib().kg_get_tile(self._h, ctypes.byref(nt), ctypes.byref(bh)))

@@ -27,6 +27,8 @@ typedef struct kg_batch_tuning {
     int chunk;  /* steps per graph (launch mode) or per persistent launch */
     int streams; /* launch mode: instances split into this many groups of about equal cells, each
                     group stepped on its own stream (1..KG_BATCH_MAX_STREAMS); 1 in persistent mode */
+    int tblock; /* temporal blocking: time steps per pass over HBM, 1 or 2 (2 needs nt <= 128; the strip
+                   is then nt - 6 columns wide and the halo 4 columns and 3 rows of phi per side) */
 } kg_batch_tuning;
 
 typedef struct kg_batch kg_batch;
@@ -46,9 +48,11 @@ KG_API int kg_batch_set_fields(kg_batch* b, int k, const double* phi, const doub
 KG_API int kg_batch_get_info(const kg_batch* b, int* n, long long* cells, long long* steps, int* nwork);
 KG_API int kg_batch_set_tuning(kg_batch* b, const kg_batch_tuning* t);
 KG_API int kg_batch_get_tuning(const kg_batch* b, kg_batch_tuning* t);
-/* Times trial_steps steps of every (nt, bh, mode) candidate on this batch,
- * installs the fastest (keeping the current chunk) and restores the state it
- * started from.  best / best_ms_per_step may be NULL. */
+/* Times trial_steps steps of every (nt, bh, mode/streams, tblock) candidate
+ * on this batch -- 120 candidates: nt 32/64/128, bh 4/8/16/32, launch mode on
+ * 1/4/8/16 streams or persistent, 1 or 2 steps per pass -- installs the
+ * fastest (keeping the current chunk) and restores the state it started from.
+ * best / best_ms_per_step may be NULL. */
 KG_API int kg_batch_autotune(kg_batch* b, int trial_steps, kg_batch_tuning* best, double* best_ms_per_step);
 KG_API int kg_batch_get_stream(kg_batch* b, void** stream);
 

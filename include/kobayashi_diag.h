@@ -41,7 +41,24 @@ KG_API int kg_diag_barrier_timeout(int blocks, long long max_polls, int* timed_o
  * flag.  *timed_out = 1 is the expected outcome. */
 KG_API int kg_diag_mbar_timeout(int* timed_out);
 
-/* Measures the FP64 FMA throughput of the current device: lane-operations per second. */
+/* Host-side fault injection: raises the handle's device error flag exactly as
+ * a step kernel whose bounded bulk-copy wait ran out does (nothing runs on the
+ * GPU, nothing faults).  The next kg_sync / kg_get_fields reports
+ * KG_ERR_TIMEOUT, and kg_step then refuses until the state is replaced. */
+KG_API int kg_diag_inject_timeout(kg_sim* h);
+
+/* FP64 pipe probe on the current device: every thread runs `chains` (4, 8 or
+ * 16) independent dependency chains of one FP64 operation -- op 0: FMA,
+ * 1: add, 2: multiply, 3: two adds per multiply -- in ctas_per_sm CTAs of
+ * `threads` threads (64..512) on every SM.  Returns lane-operations per
+ * second (CUDA events) and, if lanes_per_sm_clock is not NULL, lane-operations
+ * per SM per SM clock cycle (from clock64 stamps of every CTA, independent of
+ * the clock frequency). */
+KG_API int kg_diag_fp64_probe(int op, int chains, int ctas_per_sm, int threads, double* lanes_per_s,
+                              double* lanes_per_sm_clock);
+
+/* The highest FP64 lane-operation rate of kg_diag_fp64_probe over ops 0..3, 8 and 16 chains and 2, 4
+ * and 8 CTAs of 256 threads per SM. */
 KG_API int kg_diag_fp64_peak(double* ops_per_s);
 
 #ifdef __cplusplus

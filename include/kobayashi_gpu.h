@@ -133,7 +133,10 @@ KG_API int kg_get_stream(kg_sim* h, void** stream);
  * library (6 MiB per GPU that loads the library, held until exit), so grids
  * are limited to 262,144 cells (512 x 512); larger ones are refused with
  * KG_ERR_INVALID.  The first call on each device looks up that array's device
- * address and keeps it: make that first call before any stream capture.  All
+ * address and keeps it, and loads the step kernel: make that first call (any
+ * nsteps, 0 included) before any stream capture.  The step uses per-lane row
+ * loads only (no bulk copies, hence no bounded wait that could time out);
+ * its results are those of kg_step, its speed may differ.  All
  * calls on a device share the array, so calls that overlap on the GPU (e.g. on
  * two streams at once) race and corrupt each other; nothing in the array needs
  * to start at zero, each call overwrites what it reads.  Returns once the work
@@ -147,6 +150,16 @@ KG_API int kg_step_noalloc(int nx, int ny, const kg_params* p, double* phi, doub
  * the shape. */
 KG_API int kg_set_tile(kg_sim* h, int nt, int bh);
 KG_API int kg_get_tile(const kg_sim* h, int* nt, int* bh);
+
+/* Temporal blocking factor k of kg_step: 1 (default) advances the grid one
+ * step per pass over HBM; 2 advances it two steps per pass, holding the
+ * intermediate step in shared memory (a halo of 4 columns and 3 rows of phi
+ * each side, recomputed).  Results are identical for k = 1 and 2; k = 2 halves
+ * the HBM traffic per step and costs extra FP64 work on the halo.  An odd
+ * remainder of steps takes one k = 1 launch.  No counterpart in the reference
+ * (it sweeps the whole grid twice per step, src/Kobayashi.cpp:227-239). */
+KG_API int kg_set_tblock(kg_sim* h, int k);
+KG_API int kg_get_tblock(const kg_sim* h, int* k);
 
 /* Steps per captured CUDA graph used by kg_step (default 100; 0 = no graphs). */
 KG_API int kg_set_graph_chunk(kg_sim* h, int chunk);

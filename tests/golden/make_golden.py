@@ -19,8 +19,21 @@ shipped), on small cases, and stores what it produced:
                             these hashes; also the measured noise floor between
                             kg_math and the C library after 2000 steps
 
-Needs the reference checkout (only present where fixtures are made).
-Run from the repository root:  python tests/golden/make_golden.py [--only-kgm]
+  full_configs.json         the large workloads at full length through the oracle
+                            with kg_math (what the GPU computes): SHA-256 of the
+                            final fields of the 8192^2 grid (64 disks) at steps
+                            1000, 2000, 5000 and 10,000; of all 54 anisotropy
+                            variants on 2048^2 at 5000 steps; and of all 512
+                            instances of the mixed-size ensemble at 3000 steps.
+                            Written by --full-configs (hours of CPU time; each
+                            finished part is saved at once, and a rerun skips
+                            the parts already present)
+
+Needs the reference checkout (only present where fixtures are made), except
+for --only-kgm and --full-configs, which run the C restatement alone.
+Run from the repository root:
+  python tests/golden/make_golden.py [--only-kgm]
+  python tests/golden/make_golden.py --full-configs [--threads N] [--part grid8192|variants|ensemble]
 (--only-kgm rewrites kgm_grid300.json alone, after a change to kg_math.h)
 """
 import hashlib
@@ -64,6 +77,9 @@ def run_ref(nx, ny, params, steps, fp64=True, init=None, via_update=False):
 
 def main():
     ko_oracle.build()
+    if "--full-configs" in sys.argv[1:]:
+        write_full_configs()
+        return
     only_kgm = "--only-kgm" in sys.argv[1:]
     if only_kgm:
         write_kgm()
@@ -121,6 +137,92 @@ def write_kgm():
                         noise_floor_T=float(np.abs(a[1] - b[1]).max() / np.abs(b[1]).max()))
     with open(os.path.join(HERE, "kgm_grid300.json"), "w") as f:
         json.dump(out, f, indent=1)
+
+
+FULL = os.path.join(HERE, "full_configs.json")
+
+
+def _arg(name, default):
+    a = sys.argv[1:]
+    return a[a.index(name) + 1] if name in a else default
+
+
+def _save_full(doc):
+    tmp = FULL + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(doc, f, indent=1, sort_keys=True)
+    os.replace(tmp, FULL)
+
+
+def field_hashes(phi, t, th):
+    return dict(sha_phi=sha(phi), sha_T=sha(t), sha_theta=sha(th))
+
+
+def _variant_job(args):
+    v, threads = args
+    st = ko_oracle.port_run(*configs.initial_fields(v["nx"], v["ny"], v["disks"]), v["params"], v["steps"],
+                            libm=False, threads=threads)
+    return v["name"], field_hashes(*st)
+
+
+def _instance_job(args):
+    k, inst, steps = args
+    st = ko_oracle.port_run(*configs.initial_fields(inst["nx"], inst["ny"], inst["disks"]), inst["params"], steps,
+                            libm=False, threads=1)
+    return k, hashlib.sha256(b"".join(np.ascontiguousarray(a).tobytes() for a in st)).hexdigest()
+
+
+def write_full_configs():
+    """7: the large workloads at full length (see the module docstring)"""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import time
+    threads = int(_arg("--threads", str(os.cpu_count() or 1)))
+    part = _arg("--part", "all")
+    doc = json.load(open(FULL)) if os.path.exists(FULL) else {}
+    doc["note"] = ("oracle ko_run with kg_math (libm=0), the arithmetic the GPU reproduces; sha256 of the "
+                   "float64 little-endian bytes of each [ny, nx] field")
+    ctx = mp.get_context("spawn")
+    if part in ("all", "ensemble"):
+        cfg = configs.ensemble_512()
+        ens = doc.setdefault("ensemble_512", {"steps": cfg["steps"], "instances": {}})
+        todo = [(k, i, cfg["steps"]) for k, i in enumerate(cfg["instances"]) if str(k) not in ens["instances"]]
+        # largest first, so the pool ends on small jobs
+        todo.sort(key=lambda a: -a[1]["nx"] * a[1]["ny"])
+        t0 = time.time()
+        with cf.ProcessPoolExecutor(max_workers=threads, mp_context=ctx) as ex:
+            for n, (k, h) in enumerate(ex.map(_instance_job, todo)):
+                ens["instances"][str(k)] = h
+                if n % 32 == 31:
+                    _save_full(doc)
+        ens["what"] = "per instance: sha256 of phi, T, theta bytes concatenated, after %d steps" % cfg["steps"]
+        _save_full(doc)
+        print("ensemble_512 done in %.0f s" % (time.time() - t0), flush=True)
+    if part in ("all", "grid8192"):
+        cfg = configs.grid_8192()
+        g = doc.setdefault("grid_8192", {"disks_seed": 8192, "params": cfg["params"], "at_step": {}})
+        marks = [1000, 2000, 5000, 10000]
+        done = [int(s) for s in g["at_step"]]
+        if not all(m in done for m in marks):
+            st = configs.initial_fields(cfg["nx"], cfg["ny"], cfg["disks"])
+            at = 0
+            t0 = time.time()
+            for m in marks:
+                st = ko_oracle.port_run(*st, cfg["params"], m - at, libm=False, threads=threads)
+                at = m
+                g["at_step"][str(m)] = field_hashes(*st)
+                _save_full(doc)
+                print("grid_8192 step %d at %.0f s" % (m, time.time() - t0), flush=True)
+    if part in ("all", "variants"):
+        vs = configs.variants_2048()
+        vd = doc.setdefault("variants_2048", {"steps": vs[0]["steps"], "variants": {}})
+        todo = [(v, 1) for v in vs if v["name"] not in vd["variants"]]
+        t0 = time.time()
+        with cf.ProcessPoolExecutor(max_workers=threads, mp_context=ctx) as ex:
+            for name, h in ex.map(_variant_job, todo):
+                vd["variants"][name] = h
+                _save_full(doc)
+                print("variant %s at %.0f s" % (name, time.time() - t0), flush=True)
 
 
 if __name__ == "__main__":
