@@ -190,11 +190,11 @@ def cpu_baseline_sample(cfg, seconds_budget=20.0):
     return out
 
 
-def measure_ensemble(steps=100, trial_steps=10):
-    """The mixed-size ensemble (512 instances, sides 64..512, per-instance parameters), timed over the
-    same `steps` steps from the initial state three ways: one autotuned batched launch per step; the
-    512 instances as single-grid handles run one after another on one stream (the looped baseline);
-    and the same handles each on its own stream (concurrent single-grid runs)."""
+def measure_ensemble(steps=3000, trial_steps=10):
+    """The mixed-size ensemble (512 instances, sides 64..512, per-instance parameters), timed over its
+    whole 3000-step workload from the initial state three ways: the autotuned batched form (CUDA graphs
+    of 100 steps); the 512 instances as single-grid handles run one after another on one stream (the
+    looped baseline); and the same handles each on its own stream (concurrent single-grid runs)."""
     import torch
     from crystalgrowth_gb300 import Batch, Kobayashi, configs
     cfg = configs.ensemble_512()
@@ -209,8 +209,8 @@ def measure_ensemble(steps=100, trial_steps=10):
     t0 = time.perf_counter()
     best, _ = b.autotune(trial_steps=trial_steps)
     tune_s = time.perf_counter() - t0
-    b.set_tuning(**dict(best, chunk=steps))
-    b.step(steps)  # warm-up (graph build)
+    b.set_tuning(**dict(best, chunk=CHUNK))
+    b.step(CHUNK)  # warm-up (graph build)
     seed_batch()
     stream = torch.cuda.ExternalStream(b.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -225,8 +225,8 @@ def measure_ensemble(steps=100, trial_steps=10):
     sims = []
     for i in inst:
         s = Kobayashi(i["nx"], i["ny"], i["params"]["dt"], params=i["params"])
-        s.set_graph_chunk(steps)
-        s.step(steps)  # warm-up (graph build)
+        s.set_graph_chunk(CHUNK)
+        s.step(CHUNK)  # warm-up (graph build)
         sims.append(s)
 
     def run(sequential):
@@ -252,7 +252,7 @@ def measure_ensemble(steps=100, trial_steps=10):
             "concurrent_streams_cell_updates_per_s": work / concurrent_s,
             "speedup_vs_looped": looped_s / batched_s, "speedup_vs_concurrent_streams": concurrent_s / batched_s,
             "tuning": best, "autotune_s": tune_s,
-            "looped": "512 single-grid handles, one after another (each a CUDA graph of the %d steps)" % steps,
+            "looped": "512 single-grid handles, one after another (each in CUDA graphs of %d steps)" % CHUNK,
             "concurrent_streams": "the same 512 handles, each on its own stream, all enqueued before waiting"}
 
 
@@ -351,6 +351,8 @@ def run_ours(args, rank, world):
     for _ in range(args.warmup):
         sim.step(CHUNK)
     sim.seed_disks(cfg["disks"])
+    if args.skip_to:
+        sim.step(args.skip_to)  # untimed: the timed window starts later in the trajectory
     sim.sync()
 
     # one event at every chunk boundary: the whole timed run, and the time of each 100-step chunk
@@ -447,8 +449,8 @@ def run_ours(args, rank, world):
             "config": {"workload": "grid_%d: %dx%d FP64 Kobayashi step, %d seeded disks r=4..8, "
                                    "delta=0.02 theta0=0.2" % (nx, nx, ny, args.disks),
                        "bench_step": "one CUDA graph of %d time steps" % CHUNK,
-                       "steps_timed": "time steps 0..%d of the trajectory from the seeded state (the "
-                                      "workload is 10,000 steps)" % (args.steps * CHUNK),
+                       "steps_timed": "time steps %d..%d of the trajectory from the seeded state (the "
+                                      "workload is 10,000 steps)" % (args.skip_to, args.skip_to + args.steps * CHUNK),
                        "e2e_steps": "%d chunks continuing from the timed run's final state, after one untimed "
                                     "round trip" % e2e_steps,
                        "strips": "%d threads x %d rows" % sim.tile(),
@@ -461,7 +463,9 @@ def run_ours(args, rank, world):
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": 3 * 8 * cells,
                     "d2h_bytes_per_step": 3 * 8 * cells, "breakdown": e2e_parts},
             "gpu_launches": args.steps * CHUNK,
-            "chunk_ms": {"first": chunk_ms[0], "median": statistics.median(chunk_ms), "last": chunk_ms[-1]},
+            "chunk_ms": {"first": chunk_ms[0], "median": statistics.median(chunk_ms), "last": chunk_ms[-1],
+                         "mean_per_1000_steps": [statistics.mean(chunk_ms[k:k + 10])
+                                                 for k in range(0, len(chunk_ms), 10)]},
             "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(cfg)
@@ -487,6 +491,8 @@ def main():
     ap.add_argument("--disks", type=int, default=64)
     ap.add_argument("--tile", default="", help="strip shape NT,BH (default: the library's choice for the grid)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (short profiling runs)")
+    ap.add_argument("--skip-to", type=int, default=0,
+                    help="advance this many time steps untimed before the timed window (profiling of later windows)")
     ap.add_argument("--tblock", type=int, default=1, help="time steps per pass over HBM (1, or 2: temporal blocking)")
     args = ap.parse_args()
     rank, world = dist_init(args.gpus)

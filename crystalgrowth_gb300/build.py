@@ -79,6 +79,37 @@ def build(force=False, verbose_ptxas=False, quiet=True):
     return LIB
 
 
+# Compile-time switches of the kernels and the setting each one ships with.  Every other setting
+# computes the same bits (they exist for A/B measurements; the defaults are the measured winners).
+SWITCHES = {"KG_BITS_ASM": 1, "KG_GDIV": 1, "KG_FAR": 1, "KG_FUSE": 1, "KG_QUIET": 3, "KG_IDIV_SUBN": 1,
+            "KG_SLOW_NOINLINE": 1, "KG_TMA": 1}
+# the plain build: every shortcut and every switch in its other setting
+PLAIN = {"KG_BITS_ASM": 0, "KG_GDIV": 0, "KG_FAR": 0, "KG_FUSE": 0, "KG_QUIET": 0, "KG_IDIV_SUBN": 0,
+         "KG_SLOW_NOINLINE": 0, "KG_TMA": 0}
+
+
+def build_variant(lib_path, defines):
+    """Build the library with extra -D definitions into lib_path (object files beside it)."""
+    bdir = os.path.join(os.path.dirname(os.path.abspath(lib_path)), "_obj")
+    os.makedirs(bdir, exist_ok=True)
+    flags = ["-D%s=%s" % kv for kv in sorted(defines.items())]
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+
+    def one(src):
+        obj = os.path.join(bdir, os.path.basename(src)[:-3] + ".o")
+        r = subprocess.run([nvcc()] + cflags() + flags + ["-c", src, "-o", obj], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed on %s with %s:\n%s" % (os.path.basename(src), flags, r.stderr))
+        return obj
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(one, srcs))
+    r = subprocess.run([nvcc()] + ARCH + ["-shared", "-o", lib_path] + objs + ["-lcudart"], capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s" % r.stderr)
+    return lib_path
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv, quiet=False)
     if "-v" in sys.argv:

@@ -31,6 +31,18 @@ int kg_cuda_fail(cudaError_t e, const char* what)
 
 extern "C" const char* kg_last_error(void) { return g_err; }
 
+cudaError_t kg_copy_pieces(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s)
+{
+    const size_t piece = (size_t)64 << 20;
+    for (size_t off = 0; off < bytes; off += piece) {
+        const size_t n = bytes - off < piece ? bytes - off : piece;
+        cudaError_t e = cudaMemcpyAsync((char*)dst + off, (const char*)src + off, n, kind, s);
+        if (e != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
+}
+
 extern "C" const char* kg_version(void) { return "kobayashi-gb300 0.1 (sm_103a, FP64)"; }
 
 /* _parameterInit and the ctor's grid spacing (src/Kobayashi.cpp:61-63,76-84) */

@@ -23,6 +23,12 @@ int kg_cuda_fail(cudaError_t e, const char* what);
             return kg_cuda_fail(kg_e_, #call);                     \
     } while (0)
 
+/* A host<->device copy of `bytes`, enqueued on stream s as consecutive cudaMemcpyAsync calls of at
+ * most 64 MiB each.  Measured on GB300 (Grace host link, pinned buffers): 64 MiB pieces held 186-192
+ * GB/s in every run, while single 512 MiB copies issued right after long compute phases fell to
+ * 6-60 GB/s. */
+cudaError_t kg_copy_pieces(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s);
+
 /* fills the derived constants of one parameter set; returns KG_OK or KG_ERR_INVALID */
 int kg_prepare(const kg_params* p, KgDev* d);
 

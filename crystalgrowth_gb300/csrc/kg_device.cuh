@@ -79,9 +79,11 @@ __device__ __forceinline__ bool kg_neg_big(uint64_t b)
     return b > (0x8000000000000000ull | KG_EPS_BITS) && b <= 0xfff0000000000000ull;
 }
 
-/* 1: the quiet-cell shortcut (all-zero phi neighbourhoods, exact); 0: the plain sequence everywhere */
+/* The quiet-cell shortcut (exact; all-zero phi neighbourhoods): 0 off; 2 in the phi/T update only;
+ * 3 as 2, and stage 1 of a cell with four +0 phi neighbours skips its two differences and the angle;
+ * 1 as 3, and also settles that cell's eps eps' phi_x, eps eps' phi_y as signed zeros */
 #ifndef KG_QUIET
-#define KG_QUIET 1
+#define KG_QUIET 3
 #endif
 
 /* 1: the angle's quotient gy/gx through kg_gdiv (the IEEE bits on the integer pipes); 0: the
@@ -118,7 +120,7 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
 {
     KgS1 o;
     double gx, gy;
-#if KG_QUIET
+#if KG_QUIET == 1 || KG_QUIET == 3
     /* four +0 neighbours: both differences are +0 and the angle keeps its value (the dead zone) */
     const bool quiet = (kg_bits(pE) | kg_bits(pW) | kg_bits(pN) | kg_bits(pS)) == 0;
     if (quiet) {
@@ -176,7 +178,7 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
     o.gx = gx;
     o.gy = gy;
     o.e2 = e2;
-#if KG_QUIET
+#if KG_QUIET == 1
     if (quiet && (kg_bits(ee) & KG_ABS_MASK) < KG_INF_BITS) {
         /* ee (+0) for a finite ee: a zero with ee's sign */
         o.a = kg_from_bits(kg_bits(ee) & ~KG_ABS_MASK);
@@ -190,16 +192,6 @@ __device__ __forceinline__ KgS1 kg_stage1(const KgDev& P, double pE, double pW, 
     return o;
 }
 
-/*
- * How much of the step's FP64 arithmetic moves to the integer pipes
- * (bit-identical either way, see kg_math.h):
- *   0  the FP64 pipe does every add and multiply
- *   1  the Laplacians' doubling 2 (E+W+N+S) is an exponent increment
- *   2  as 1, and the Laplacians' eight neighbour additions use kg_iadd
- */
-#ifndef KG_EMU
-#define KG_EMU 0
-#endif
 /* 1: kg_twice_plus in the Laplacians and the T bound for m (both exact); 0: the plain sequence */
 #ifndef KG_FUSE
 #define KG_FUSE 1
@@ -214,12 +206,7 @@ __device__ __forceinline__ double kg_lap(const KgDev& P, double c, double e, dou
                                          double sw, double nw, double se)
 {
     double v;
-#if KG_EMU >= 2
-    double s4 = kg_iadd(kg_iadd(kg_iadd(e, w), n), s);
-    v = kg_iadd(kg_iadd(kg_iadd(kg_iadd(kg_imul2(s4), ne), sw), nw), se) - 12.0 * c;
-#elif KG_EMU == 1
-    v = kg_imul2(e + w + n + s) + ne + sw + nw + se - 12.0 * c;
-#elif KG_FUSE
+#if KG_FUSE
     v = kg_twice_plus(e + w + n + s, ne) + sw + nw + se - 12.0 * c;
 #else
     v = 2.0 * (e + w + n + s) + ne + sw + nw + se - 12.0 * c;

@@ -8,7 +8,7 @@
 #include "kobayashi_diag.h"
 
 __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double* __restrict__ y, long long n, double b,
-                                    double yh, double yl, kg_idivc ic)
+                                    kg_idivc ic)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         double v = x[i], r = 0.0;
@@ -18,18 +18,8 @@ __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double
             double s, c;
             kg_sincos(v, &s, &c);
             r = fn == KG_FN_SIN ? s : c;
-        } else if (fn == KG_FN_CDIV) {
-            r = kg_cdiv(v, b, yh, yl);
         } else if (fn == KG_FN_IDIV) {
             r = kg_idiv(v, &ic);
-        } else if (fn == KG_FN_IADD) {
-            r = kg_iadd(v, x[n - 1 - i]);
-        } else if (fn == KG_FN_ADD) {
-            r = __dadd_rn(v, x[n - 1 - i]);
-        } else if (fn == KG_FN_IMUL2) {
-            r = kg_imul2(v);
-        } else if (fn == KG_FN_MUL2) {
-            r = __dmul_rn(2.0, v);
         } else if (fn == KG_FN_DIV) {
             r = v / b;
         } else if (fn == KG_FN_TWICE_PLUS) {
@@ -47,13 +37,14 @@ __global__ void kg_diag_eval_kernel(int fn, const double* __restrict__ x, double
 
 extern "C" int kg_diag_eval(int fn, const double* x, double* y, long long n, double b)
 {
-    if (fn < KG_FN_ATAN || fn > KG_FN_DIV_PAIR || fn == 12 || n < 0 || (n > 0 && (!x || !y)))
+    const bool known = fn == KG_FN_ATAN || fn == KG_FN_SIN || fn == KG_FN_COS || fn == KG_FN_DIV ||
+                       fn == KG_FN_IDIV || fn == KG_FN_TWICE_PLUS || fn == KG_FN_MUL2_ADD || fn == KG_FN_GDIV ||
+                       fn == KG_FN_DIV_PAIR;
+    if (!known || n < 0 || (n > 0 && (!x || !y)))
         return kg_fail(KG_ERR_INVALID, "kg_diag_eval: bad arguments");
-    double yh = 0, yl = 0;
     kg_idivc ic;
     memset(&ic, 0, sizeof ic);
-    if ((fn == KG_FN_CDIV || fn == KG_FN_DIV || fn == KG_FN_IDIV) &&
-        (kg_cdiv_prepare(b, &yh, &yl) || kg_idiv_prepare(b, &ic)))
+    if ((fn == KG_FN_DIV || fn == KG_FN_IDIV) && kg_idiv_prepare(b, &ic))
         return kg_fail(KG_ERR_INVALID, "kg_diag_eval: divisor outside [2^-100, 2^100]");
     if (n == 0)
         return KG_OK;
@@ -62,7 +53,7 @@ extern "C" int kg_diag_eval(int fn, const double* x, double* y, long long n, dou
     cudaError_t e = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         int blocks = (int)((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8);
-        kg_diag_eval_kernel<<<blocks, 256>>>(fn, d, d + n, n, b, yh, yl, ic);
+        kg_diag_eval_kernel<<<blocks, 256>>>(fn, d, d + n, n, b, ic);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)

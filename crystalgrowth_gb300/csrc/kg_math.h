@@ -17,24 +17,19 @@
  * gen_kg_math_tables.py, which evaluates the mathematics in 320-bit precision):
  *   kg_atan   table-driven Taylor expansion around c_k = k/128 (Gal's
  *             accurate-tables method), argument reduction atan(x) =
- *             pi/2 - atan(1/x) for |x| > 1; kg_atan_x evaluates it in 64-bit
- *             fixed point on the integer pipes (the step's version),
- *             kg_atan_f64 in FP64 with a Newton-refined reciprocal.
+ *             pi/2 - atan(1/x) for |x| > 1, evaluated in 64-bit fixed point on
+ *             the integer pipes (kg_atan_x).
  *   kg_sincos sin(nh + r) = S_n cos r + C_n sin r, h = pi/128, with tabulated
  *             S_n, C_n: kg_sincos_x reduces |x| < 64 exactly with a 192-bit
  *             product by 128/pi (Payne-Hanek style) and works in fixed point;
- *             kg_sincos_f64 uses a three-part Cody-Waite reduction in FP64.
- *   kg_gdiv   the IEEE quotient a/b for any divisor on the integer pipes.
- *   kg_cdiv   division by a divisor b fixed for a whole run: Markstein's
- *             correction q = q0 + (a - b q0) * RN(1/b) applied to a faithful
- *             quotient q0 = a * (1/b as a hi+lo pair); returns RN(a/b), i.e.
- *             the same bits as the IEEE division a/b (Markstein 1990; the
- *             hi+lo reciprocal makes q0 faithful).  Subnormal, huge and
- *             non-finite dividends fall back to a/b.
+ *             64 <= |x| < 4096 takes kg_sincos_f64, a three-part Cody-Waite
+ *             reduction in FP64.
+ *   kg_idiv   the IEEE quotient a/b for a divisor fixed for a whole run, and
+ *   kg_gdiv   for any divisor, both on the integer pipes.
  *
  * Accuracy: kg_atan_x < 0.55 ulp; kg_sincos_x absolute error < 2^-61 and
- * faithful where |value| >= 2^-9; the FP64 formulations about 1 ulp;
- * kg_sincos requires |x| < 4096 and returns NaN outside.
+ * faithful where |value| >= 2^-9; kg_sincos_f64 about 1 ulp; kg_sincos
+ * returns NaN for |x| >= 4096.
  *
  * This header is C99 and CUDA C++ at the same time (the oracle is plain C).
  */
@@ -200,18 +195,6 @@ KG_HD float kg_rcp_f(float x)
 #endif
 }
 
-/* correctly rounded FP32 reciprocal of a correctly rounded FP32 conversion */
-KG_HD double kg_rcp_seed(double x)
-{
-#if defined(__CUDA_ARCH__)
-    return (double)__frcp_rn(__double2float_rn(x));
-#else
-    float xf = (float)x;
-    float r = 1.0f / xf;
-    return (double)r;
-#endif
-}
-
 /* round-to-nearest-even of an FP32 value to int (|v| < 2^23) */
 KG_HD int kg_rint_f(float v)
 {
@@ -220,62 +203,6 @@ KG_HD int kg_rint_f(float v)
 #else
     return (int)lrintf(v);
 #endif
-}
-
-/*
- * atan(x) in FP64 arithmetic, faithful for every double (NaN propagates).
- *   |x| <= 1 : t = |x|
- *   |x| > 1  : t + tlo = 1/|x| (Newton-refined FP32 seed), result pi/2 - atan(t)
- *   k = nearest node of t on the grid k/128, d = t - k/128 (exact), |d| <= 1/256
- *   atan(t) = A_k + d * P_k(d), P_k the degree-6 Horner tail of the Taylor series
- */
-KG_HD double kg_atan_f64(double x)
-{
-    /* comparisons on the bit pattern: exact, and off the FP64 pipe on the GPU */
-    uint64_t ux = kg_bits(x);
-    uint64_t ua = ux & 0x7fffffffffffffffull;
-    double ax = kg_from_bits(ua);
-    if (ua > 0x43f0000000000000ull) {          /* |x| > 2^64, inf or NaN */
-        if (ua > 0x7ff0000000000000ull)
-            return kg_add_slow(x, x);
-        return (ux >> 63) ? -KG_PIO2_HI : KG_PIO2_HI;
-    }
-    double t, tlo = 0.0;
-    int inv = ua > 0x3ff0000000000000ull;      /* |x| > 1 */
-    if (inv) {
-        double y0 = kg_rcp_seed(ax);
-        double e0 = kg_fma(-ax, y0, 1.0);
-        double y1 = kg_fma(y0, e0, y0);
-        double e1 = kg_fma(-ax, y1, 1.0);
-        t = y1;
-        tlo = y1 * e1;
-    } else {
-        t = ax;
-    }
-#if defined(__CUDA_ARCH__)
-    int k = (int)__fadd_rn(__fmul_rn(__double2float_rn(t), (float)KG_ATAN_N), 0.5f);
-#else
-    float tf = (float)t;
-    float tk = tf * (float)KG_ATAN_N;
-    int k = (int)(tk + 0.5f);
-#endif
-    int b = k * KG_ATAN_STRIDE;
-    double d = t - kg_tab_atan(b + 0);
-    if (inv)
-        d = d + tlo;
-    double p = kg_tab_atan(b + 11);
-    p = kg_fma(d, p, kg_tab_atan(b + 10));
-    p = kg_fma(d, p, kg_tab_atan(b + 9));
-    p = kg_fma(d, p, kg_tab_atan(b + 8));
-    p = kg_fma(d, p, kg_tab_atan(b + 7));
-    p = kg_fma(d, p, kg_tab_atan(b + 6));
-    p = kg_fma(d, p, kg_tab_atan(b + 5));
-    double r;
-    if (inv)
-        r = kg_tab_atan(b + 3) + kg_fma(-d, p, kg_tab_atan(b + 4));
-    else
-        r = kg_tab_atan(b + 1) + kg_fma(d, p, kg_tab_atan(b + 2));
-    return (ux >> 63) ? -r : r;
 }
 
 /*
@@ -327,49 +254,6 @@ KG_HD void kg_sincos_f64(double x, double* s_out, double* c_out)
     *c_out = ch + ct;
 }
 
-/*
- * Reciprocal pair for kg_cdiv: yh = RN(1/b), yl = RN((1 - b*yh)/b).
- * Valid for 2^-100 <= b <= 2^100; returns 0 on success, -1 otherwise.
- */
-KG_HD int kg_cdiv_prepare(double b, double* yh, double* yl)
-{
-    if (!(b >= 0x1p-100 && b <= 0x1p100))
-        return -1;
-    double h = 1.0 / b;
-    double e = kg_fma(-b, h, 1.0); /* exact: 1 - b*h fits in 53 bits */
-    *yh = h;
-    *yl = e / b;
-    return 0;
-}
-
-/*
- * a / b with the bits of the IEEE division, for a divisor b prepared by
- * kg_cdiv_prepare: 4 double operations instead of the ~8 of a general
- * division.  Normal dividends below 2^899 take this path -- those under
- * 2^-900 lifted by 2^200 first and the quotient scaled back (both exact
- * exponent-field adjustments) -- and so do zeros (0/b = 0 with a's sign);
- * subnormal, huge, infinite and NaN dividends, and tiny dividends whose
- * quotient would be subnormal, take the IEEE division itself.
- */
-KG_HD double kg_cdiv(double a, double b, double yh, double yl)
-{
-    uint64_t ua = kg_bits(a);
-    uint64_t ea = (ua >> 52) & 0x7ff;
-    int zero = (ua & 0x7fffffffffffffffull) == 0;
-    if (ea - 1u < 1921u || zero) {
-        uint64_t sh = (ea < 123u) ? (200ull << 52) : 0ull;
-        double as = kg_from_bits(ua + sh);
-        double q0 = kg_fma(as, yh, as * yl);
-        double r = kg_fma(-q0, b, as);
-        double q = kg_fma(r, yh, q0);
-        uint64_t uq = kg_bits(q);
-        if (zero)
-            return a;
-        if (sh == 0 || ((uq >> 52) & 0x7ff) > 200u)
-            return kg_from_bits(uq - sh);
-    }
-    return kg_div_slow(a, b);
-}
 
 
 /*
@@ -514,76 +398,6 @@ KG_HD double kg_idiv(double a, const kg_idivc* c)
 }
 
 
-
-/*
- * a + b (IEEE binary64, round to nearest even) in 64-bit integer arithmetic,
- * the same bits as the hardware addition; infinite and NaN operands take the
- * hardware path.  Significands carry 10 guard bits (hidden bit at bit 62);
- * bits shifted out of the smaller operand fold into a sticky bit; an exact
- * cancellation gives +0; results below 2^-1022 stay exact (subnormal).
- */
-KG_HD double kg_iadd(double a, double b)
-{
-    uint64_t ua = kg_bits(a), ub = kg_bits(b);
-    uint64_t aa = ua & 0x7fffffffffffffffull, ab = ub & 0x7fffffffffffffffull;
-    if (aa >= 0x7ff0000000000000ull || ab >= 0x7ff0000000000000ull)
-        return kg_add_slow(a, b);
-    int swap = ab > aa;
-    uint64_t ux = swap ? ub : ua, uy = swap ? ua : ub;
-    uint64_t ax = swap ? ab : aa, ay = swap ? aa : ab;
-    int ex = (int)(ax >> 52), ey = (int)(ay >> 52);
-    uint64_t mx = ((ax & 0x000fffffffffffffull) | (ex ? 0x0010000000000000ull : 0)) << 10;
-    uint64_t my = ((ay & 0x000fffffffffffffull) | (ey ? 0x0010000000000000ull : 0)) << 10;
-    ex += ex == 0;
-    ey += ey == 0;
-    int d = ex - ey;
-    uint64_t myal;
-    if (d >= 64)
-        myal = my != 0;
-    else if (d > 0)
-        myal = (my >> d) | ((my << (64 - d)) != 0);
-    else
-        myal = my;
-    uint64_t sign = ux & 0x8000000000000000ull;
-    int e = ex;
-    uint64_t mm;
-    if (((ux ^ uy) >> 63) == 0) {
-        mm = mx + myal;
-        if (mm >> 63) {
-            mm = (mm >> 1) | (mm & 1);
-            e += 1;
-        }
-    } else {
-        mm = mx - myal;
-        if (mm == 0)
-            return 0.0;
-        int lz = kg_clz64(mm) - 1;
-        if (lz > e - 1)
-            lz = e - 1;
-        mm <<= lz;
-        e -= lz;
-    }
-    if (e >= 2047)
-        return kg_from_bits(sign | 0x7ff0000000000000ull);
-    uint64_t rb = mm & 0x3ff;
-    uint64_t q = mm >> 10;
-    q += (rb > 0x200) | ((rb == 0x200) & (q & 1));
-    return kg_from_bits(sign | (((uint64_t)(e - 1) << 52) + q));
-}
-
-
-/* 2 x, exactly, by an exponent-field increment (subnormals shift their
- * significand; exponent 2046, infinities and NaN take the hardware path) */
-KG_HD double kg_imul2(double x)
-{
-    uint64_t u = kg_bits(x);
-    uint64_t a = u & 0x7fffffffffffffffull;
-    if (a >= 0x7fe0000000000000ull)
-        return kg_add_slow(x, x);
-    if (a < 0x0010000000000000ull)
-        return kg_from_bits((u & 0x8000000000000000ull) | (a << 1));
-    return kg_from_bits(u + 0x0010000000000000ull);
-}
 
 /* RN(RN(2 s) + y), the reference's "2.0 * s + y", in one FMA.  2 s is exact
  * unless it overflows, so the two roundings reduce to the FMA's one.  The
@@ -922,27 +736,9 @@ KG_HD void kg_sincos_x(double x, double* s_out, double* c_out)
     *c_out = kg_q62_to_double(cs, 0);
 }
 
-/* the functions the step uses: 1 = the integer-pipe versions, 0 = the FP64 versions */
-#ifndef KG_XMATH
-#define KG_XMATH 1
-#endif
+/* the functions the step uses: the integer-pipe versions */
+KG_HD double kg_atan(double x) { return kg_atan_x(x); }
 
-KG_HD double kg_atan(double x)
-{
-#if KG_XMATH
-    return kg_atan_x(x);
-#else
-    return kg_atan_f64(x);
-#endif
-}
-
-KG_HD void kg_sincos(double x, double* s_out, double* c_out)
-{
-#if KG_XMATH
-    kg_sincos_x(x, s_out, c_out);
-#else
-    kg_sincos_f64(x, s_out, c_out);
-#endif
-}
+KG_HD void kg_sincos(double x, double* s_out, double* c_out) { kg_sincos_x(x, s_out, c_out); }
 
 #endif /* KG_MATH_H */

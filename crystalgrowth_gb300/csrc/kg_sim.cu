@@ -16,15 +16,7 @@
 #include "kobayashi_diag.h"
 
 
-/* resident CTAs per SM the register allocation must allow (0: the compiler's choice) */
-#ifndef KG_MIN_CTAS
-#define KG_MIN_CTAS 0
-#endif
-#if KG_MIN_CTAS > 0
-#define KG_STEP_BOUNDS(NT) __launch_bounds__(NT, KG_MIN_CTAS * 128 / NT)
-#else
 #define KG_STEP_BOUNDS(NT) __launch_bounds__(NT)
-#endif
 
 /* rows of phi and T reach shared memory by bulk (TMA) copies where the strip allows it (1), or by
  * per-lane loads everywhere (0) */
@@ -443,7 +435,7 @@ extern "C" int kg_get_fields(kg_sim* h, double* phi, double* T, double* theta)
     double* dst[3] = {phi, T, theta};
     for (int f = 0; f < 3; f++)
         if (dst[f])
-            KG_CUDA(cudaMemcpyAsync(dst[f], h->buf[h->cur][f], bytes, cudaMemcpyDeviceToHost, h->stream));
+            KG_CUDA(kg_copy_pieces(dst[f], h->buf[h->cur][f], bytes, cudaMemcpyDeviceToHost, h->stream));
     return sync_and_check(h);
 }
 
@@ -456,7 +448,7 @@ extern "C" int kg_set_fields(kg_sim* h, const double* phi, const double* T, cons
     const double* src[3] = {phi, T, theta};
     for (int f = 0; f < 3; f++)
         if (src[f])
-            KG_CUDA(cudaMemcpyAsync(h->buf[h->cur][f], src[f], bytes, cudaMemcpyHostToDevice, h->stream));
+            KG_CUDA(kg_copy_pieces(h->buf[h->cur][f], src[f], bytes, cudaMemcpyHostToDevice, h->stream));
     KG_CUDA(cudaStreamSynchronize(h->stream));
     if (phi && T && theta)
         h->failed = false; /* the whole state was replaced */
@@ -535,7 +527,7 @@ extern "C" int kg_colormap(kg_sim* h, int order, float* rgba)
     rc = kg_color_launch(h->buf[h->cur][0], h->color, h->nx, h->ny, order, h->stream);
     if (rc)
         return rc;
-    KG_CUDA(cudaMemcpyAsync(rgba, h->color, bytes, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(kg_copy_pieces(rgba, h->color, bytes, cudaMemcpyDeviceToHost, h->stream));
     KG_CUDA(cudaStreamSynchronize(h->stream));
     return KG_OK;
 }
@@ -597,8 +589,8 @@ extern "C" int kg_save(kg_sim* h, const char* path)
     if (rc == KG_OK && fwrite(hdr, 1, sizeof hdr, f) != sizeof hdr)
         rc = kg_fail(KG_ERR_INVALID, "kg_save: write failed");
     for (int fld = 0; fld < 3 && rc == KG_OK; fld++) {
-        cudaError_t e = cudaMemcpyAsync(buf, h->buf[h->cur][fld], cells * sizeof(double), cudaMemcpyDeviceToHost,
-                                        h->stream);
+        cudaError_t e = kg_copy_pieces(buf, h->buf[h->cur][fld], cells * sizeof(double), cudaMemcpyDeviceToHost,
+                                       h->stream);
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(h->stream);
         if (e != cudaSuccess)
@@ -687,8 +679,8 @@ extern "C" int kg_load(kg_sim* h, const char* path)
             rc = kg_fail(KG_ERR_INVALID, "kg_load: %s is truncated", path);
             break;
         }
-        cudaError_t e = cudaMemcpyAsync(h->buf[h->cur][fld], buf, cells * sizeof(double), cudaMemcpyHostToDevice,
-                                        h->stream);
+        cudaError_t e = kg_copy_pieces(h->buf[h->cur][fld], buf, cells * sizeof(double), cudaMemcpyHostToDevice,
+                                       h->stream);
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(h->stream);
         if (e != cudaSuccess)

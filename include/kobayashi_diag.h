@@ -16,13 +16,8 @@ extern "C" {
 #define KG_FN_ATAN 0  /* y = kg_atan(x) */
 #define KG_FN_SIN 1   /* y = sin part of kg_sincos(x) */
 #define KG_FN_COS 2   /* y = cos part of kg_sincos(x) */
-#define KG_FN_CDIV 3  /* y = kg_cdiv(x, b): x / b through the constant-divisor path */
 #define KG_FN_DIV 4   /* y = x / b, the GPU's own IEEE division */
 #define KG_FN_IDIV 5  /* y = kg_idiv(x, b): x / b through the integer-pipe path */
-#define KG_FN_IADD 6  /* y[i] = kg_iadd(x[i], x[n-1-i]): integer-pipe addition */
-#define KG_FN_ADD 7   /* y[i] = x[i] + x[n-1-i], the hardware addition */
-#define KG_FN_IMUL2 8 /* y = kg_imul2(x): 2 x by an exponent increment */
-#define KG_FN_MUL2 9  /* y = 2 x, the hardware multiplication */
 #define KG_FN_TWICE_PLUS 10 /* y[i] = kg_twice_plus(x[i], x[n-1-i]): 2 x + y in one FMA */
 #define KG_FN_MUL2_ADD 11   /* y[i] = 2 x[i] + x[n-1-i], two hardware roundings */
 #define KG_FN_GDIV 13       /* y[i] = kg_gdiv(x[i], x[n-1-i]): integer-pipe division, any divisor */

@@ -194,38 +194,13 @@ int ko_run(int nx, int ny, const ko_params* p, double* phi, double* t, double* t
 /* kg_math.h entry points, for the elementary-function tests */
 double ko_kg_atan(double x) { return kg_atan(x); }
 void ko_kg_sincos(double x, double* s, double* c) { kg_sincos(x, s, c); }
-double ko_kg_cdiv(double a, double b)
-{
-    double yh, yl;
-    if (kg_cdiv_prepare(b, &yh, &yl))
-        return a / b;
-    return kg_cdiv(a, b, yh, yl);
-}
-/* n quotients a[i] / b through kg_cdiv; returns how many differ in bits from a[i] / b */
-long long ko_kg_cdiv_check(const double* a, long long n, double b)
-{
-    double yh, yl;
-    if (kg_cdiv_prepare(b, &yh, &yl))
-        return -1;
-    long long bad = 0;
-    for (long long i = 0; i < n; i++) {
-        double q = kg_cdiv(a[i], b, yh, yl);
-        double r = a[i] / b;
-        if (kg_bits(q) != kg_bits(r))
-            bad++;
-    }
-    return bad;
-}
-
-/* host evaluation of kg_math.h over an array: fn 0 atan, 1 sin, 2 cos, 3 kg_cdiv(x, b), 4 x / b,
- * 5 kg_idiv(x, b), 6 kg_iadd(x[i], x[n-1-i]), 7 x[i] + x[n-1-i], 8 kg_imul2(x), 9 2 x,
+/* host evaluation of kg_math.h over an array: fn 0 atan, 1 sin, 2 cos, 4 x / b, 5 kg_idiv(x, b),
  * 10 kg_twice_plus(x[i], x[n-1-i]), 11 2 x[i] + x[n-1-i] (two roundings), 12 kg_absorb_bound(x),
- * 13 kg_gdiv(x[i], x[n-1-i]), 14 x[i] / x[n-1-i], 15 kg_atan_f64(x) */
+ * 13 kg_gdiv(x[i], x[n-1-i]), 14 x[i] / x[n-1-i] */
 int ko_kg_eval(int fn, const double* x, double* y, long long n, double b)
 {
-    double yh = 0, yl = 0;
     kg_idivc ic;
-    if ((fn == 3 || fn == 4 || fn == 5) && (kg_cdiv_prepare(b, &yh, &yl) || kg_idiv_prepare(b, &ic)))
+    if ((fn == 4 || fn == 5) && kg_idiv_prepare(b, &ic))
         return -1;
     for (long long i = 0; i < n; i++) {
         double s, c;
@@ -233,19 +208,13 @@ int ko_kg_eval(int fn, const double* x, double* y, long long n, double b)
         case 0: y[i] = kg_atan(x[i]); break;
         case 1: kg_sincos(x[i], &s, &c); y[i] = s; break;
         case 2: kg_sincos(x[i], &s, &c); y[i] = c; break;
-        case 3: y[i] = kg_cdiv(x[i], b, yh, yl); break;
         case 4: y[i] = x[i] / b; break;
         case 5: y[i] = kg_idiv(x[i], &ic); break;
-        case 6: y[i] = kg_iadd(x[i], x[n - 1 - i]); break;
-        case 7: y[i] = x[i] + x[n - 1 - i]; break;
-        case 8: y[i] = kg_imul2(x[i]); break;
-        case 9: y[i] = 2.0 * x[i]; break;
         case 10: y[i] = kg_twice_plus(x[i], x[n - 1 - i]); break;
         case 11: y[i] = 2.0 * x[i] + x[n - 1 - i]; break;
         case 12: y[i] = kg_from_bits(kg_absorb_bound(x[i])); break;
         case 13: y[i] = kg_gdiv(x[i], x[n - 1 - i]); break;
         case 14: y[i] = x[i] / x[n - 1 - i]; break;
-        case 15: y[i] = kg_atan_f64(x[i]); break;
         default: return -1;
         }
     }

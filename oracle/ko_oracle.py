@@ -52,10 +52,6 @@ def port_lib():
         lib.ko_kg_atan.argtypes = [ctypes.c_double]
         lib.ko_kg_atan.restype = ctypes.c_double
         lib.ko_kg_sincos.argtypes = [ctypes.c_double, _dp, _dp]
-        lib.ko_kg_cdiv.argtypes = [ctypes.c_double, ctypes.c_double]
-        lib.ko_kg_cdiv.restype = ctypes.c_double
-        lib.ko_kg_cdiv_check.argtypes = [_dp, ctypes.c_longlong, ctypes.c_double]
-        lib.ko_kg_cdiv_check.restype = ctypes.c_longlong
         lib.ko_kg_eval.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_longlong, ctypes.c_double]
         lib.ko_kg_eval.restype = ctypes.c_int
         lib.ko_tlm_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(KoParams), _dp, _dp, _dp, _dp,
@@ -109,17 +105,13 @@ def kg_sincos(x):
 
 
 def kg_eval(fn, x, b=1.0):
-    """host kg_math over an array: fn 0 atan, 1 sin, 2 cos, 3 kg_cdiv(x, b), 4 x / b"""
+    """host kg_math over an array: fn 0 atan, 1 sin, 2 cos, 4 x / b, 5 kg_idiv(x, b), 10 kg_twice_plus,
+    11 two-rounding 2x + y, 12 kg_absorb_bound, 13 kg_gdiv, 14 x[i] / x[n-1-i] (see ko_oracle.c)"""
     x = np.ascontiguousarray(x, dtype=np.float64)
     y = np.empty_like(x)
     if port_lib().ko_kg_eval(int(fn), _ptr(x), _ptr(y), x.size, float(b)) != 0:
         raise ValueError("ko_kg_eval failed")
     return y
-
-
-def kg_cdiv_mismatches(a, b):
-    a = np.ascontiguousarray(a, dtype=np.float64)
-    return port_lib().ko_kg_cdiv_check(_ptr(a), a.size, float(b))
 
 
 class Reference:
