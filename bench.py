@@ -122,12 +122,15 @@ def profile_traffic():
 
 
 def fp64_peak():
-    """FP64 FMA lane-operations per second of this GPU, measured now (kg_diag_fp64_peak)."""
+    """FP64 lane-operations per second of this GPU, measured now: the best of kg_diag_fp64_peak's sweep
+    (FMA, add, multiply and the step's add/multiply mix; 8 or 16 chains; 2-8 CTAs per SM), and the
+    lanes per SM clock of the add/multiply mix (clock64 stamps, independent of the clock rate)."""
     import ctypes
     from crystalgrowth_gb300 import _lib
-    v = ctypes.c_double()
+    v, a, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
     _lib.check(_lib.lib().kg_diag_fp64_peak(ctypes.byref(v)))
-    return v.value
+    _lib.check(_lib.lib().kg_diag_fp64_probe(3, 8, 4, 256, ctypes.byref(a), ctypes.byref(c)))
+    return v.value, c.value
 
 
 def cpu_baseline_sample(cfg, seconds_budget=20.0):
@@ -419,15 +422,16 @@ def run_ours(args, rank, world):
     traffic, prof = profile_traffic()
     # the FP64 pipe's share at the time steps whose FP64-pipe load ncu measured (per cell, on 4096^2
     # with the same disk density and strip shape): lane-slots = warp instructions on the FP64 pipe x 32,
-    # against the full-warp DFMA lane rate measured now; the time is that step's chunk, from the events
+    # against the probe's lane rate measured now; the time is that step's chunk, from the events
     fp64 = None
     samples = prof.get("fp64_lane_slots_per_cell_at_step", {}) if nx == 8192 and ny == 8192 else {}
     pts = []
     pk = None
     for step, opc in sorted((int(k), float(v)) for k, v in samples.items()):
-        k = step // CHUNK
-        if k < len(chunk_ms):
-            pk = pk or fp64_peak()
+        k = (step - args.skip_to) // CHUNK
+        if 0 <= k < len(chunk_ms):
+            if pk is None:
+                pk, per_clk = fp64_peak()
             t = chunk_ms[k] / 1e3 / CHUNK
             pts.append({"step": step, "lane_slots_per_cell_update": opc, "achieved": opc * cells / t / 1e9,
                         "frac": opc * cells / t / pk})
@@ -439,7 +443,9 @@ def run_ours(args, rank, world):
             for q in pts:
                 q["frac_of_nominal"] = q["achieved"] * 1e9 / nominal
         fp64 = {"bound": "fp64 pipe", "unit": "G lane-slots/s", "peak": pk / 1e9,
-                "peak_kind": "measured now (kg_diag_fp64_peak, full-warp DFMA lanes/s)",
+                "peak_kind": "measured now (kg_diag_fp64_peak: best of FMA/add/multiply/mix dependency-chain "
+                             "loops over chains and CTAs per SM)",
+                "probe_lanes_per_sm_clock": per_clk,
                 "nominal": nominal / 1e9 if nominal else None, "at_steps": pts,
                 "ops_source": "ncu sm__inst_executed_pipe_fp64 x 32 per cell at those steps "
                               "(profiles/kg_step_kernel_traffic.json)"}

@@ -616,7 +616,7 @@ extern "C" int kg_batch_get_fields(kg_batch* b, int k, double* phi, double* T, d
     double* dst[3] = {phi, T, theta};
     for (int f = 0; f < 3; f++)
         if (dst[f])
-            KG_CUDA(kg_copy_pieces(dst[f], a + f * cells, sizeof(double) * cells, cudaMemcpyDeviceToHost, b->stream));
+            KG_CUDA(kg_copy_host(dst[f], a + f * cells, sizeof(double) * cells, cudaMemcpyDeviceToHost, b->stream));
     KG_CUDA(cudaStreamSynchronize(b->stream));
     return KG_OK;
 }
@@ -632,7 +632,7 @@ extern "C" int kg_batch_set_fields(kg_batch* b, int k, const double* phi, const 
     const double* src[3] = {phi, T, theta};
     for (int f = 0; f < 3; f++)
         if (src[f])
-            KG_CUDA(kg_copy_pieces(a + f * cells, src[f], sizeof(double) * cells, cudaMemcpyHostToDevice, b->stream));
+            KG_CUDA(kg_copy_host(a + f * cells, src[f], sizeof(double) * cells, cudaMemcpyHostToDevice, b->stream));
     KG_CUDA(cudaStreamSynchronize(b->stream));
     if (phi && T && theta)
         batch_replaced(b, k);

@@ -272,3 +272,36 @@ extern "C" int kg_diag_mbar_timeout(int* timed_out)
     *timed_out = h != 0;
     return KG_OK;
 }
+
+/* Copies `bytes` (a multiple of 16, both ends 16-byte aligned) with SM loads and stores instead of a
+ * copy engine: the GPU writes the destination directly (for page-locked host memory, over the host
+ * link). */
+__global__ void kg_diag_copy_kernel(uint4* __restrict__ dst, const uint4* __restrict__ src, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+extern "C" int kg_diag_copy(void* dst, const void* src, long long bytes, void* stream)
+{
+    if (!dst || !src || bytes < 0 || (bytes & 15) || ((uintptr_t)dst & 15) || ((uintptr_t)src & 15))
+        return kg_fail(KG_ERR_INVALID, "kg_diag_copy: pointers must be 16-byte aligned and bytes a multiple of 16");
+    /* both ends must be addresses the device can use: device memory, or page-locked host memory (whose
+     * device address is looked up, not assumed) */
+    void* ends[2] = {dst, (void*)src};
+    for (int k = 0; k < 2; k++) {
+        cudaPointerAttributes a;
+        KG_CUDA(cudaPointerGetAttributes(&a, ends[k]));
+        if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeHost && a.type != cudaMemoryTypeManaged)
+            return kg_fail(KG_ERR_INVALID, "kg_diag_copy: %s is not device or page-locked host memory",
+                           k ? "src" : "dst");
+        if (!a.devicePointer)
+            return kg_fail(KG_ERR_INVALID, "kg_diag_copy: %s has no device address", k ? "src" : "dst");
+        ends[k] = a.devicePointer;
+    }
+    if (bytes == 0)
+        return KG_OK;
+    kg_diag_copy_kernel<<<152 * 8, 256, 0, (cudaStream_t)stream>>>((uint4*)ends[0], (const uint4*)ends[1], bytes / 16);
+    KG_CUDA(cudaGetLastError());
+    return KG_OK;
+}

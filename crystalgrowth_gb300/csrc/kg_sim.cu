@@ -435,7 +435,7 @@ extern "C" int kg_get_fields(kg_sim* h, double* phi, double* T, double* theta)
     double* dst[3] = {phi, T, theta};
     for (int f = 0; f < 3; f++)
         if (dst[f])
-            KG_CUDA(kg_copy_pieces(dst[f], h->buf[h->cur][f], bytes, cudaMemcpyDeviceToHost, h->stream));
+            KG_CUDA(kg_copy_host(dst[f], h->buf[h->cur][f], bytes, cudaMemcpyDeviceToHost, h->stream));
     return sync_and_check(h);
 }
 
@@ -448,7 +448,7 @@ extern "C" int kg_set_fields(kg_sim* h, const double* phi, const double* T, cons
     const double* src[3] = {phi, T, theta};
     for (int f = 0; f < 3; f++)
         if (src[f])
-            KG_CUDA(kg_copy_pieces(h->buf[h->cur][f], src[f], bytes, cudaMemcpyHostToDevice, h->stream));
+            KG_CUDA(kg_copy_host(h->buf[h->cur][f], src[f], bytes, cudaMemcpyHostToDevice, h->stream));
     KG_CUDA(cudaStreamSynchronize(h->stream));
     if (phi && T && theta)
         h->failed = false; /* the whole state was replaced */
@@ -527,7 +527,7 @@ extern "C" int kg_colormap(kg_sim* h, int order, float* rgba)
     rc = kg_color_launch(h->buf[h->cur][0], h->color, h->nx, h->ny, order, h->stream);
     if (rc)
         return rc;
-    KG_CUDA(kg_copy_pieces(rgba, h->color, bytes, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(kg_copy_host(rgba, h->color, bytes, cudaMemcpyDeviceToHost, h->stream));
     KG_CUDA(cudaStreamSynchronize(h->stream));
     return KG_OK;
 }

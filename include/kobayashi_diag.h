@@ -56,6 +56,12 @@ KG_API int kg_diag_fp64_probe(int op, int chains, int ctas_per_sm, int threads, 
  * and 8 CTAs of 256 threads per SM. */
 KG_API int kg_diag_fp64_peak(double* ops_per_s);
 
+/* Copies `bytes` (a multiple of 16; both pointers 16-byte aligned) from src to dst with a kernel's
+ * loads and stores instead of a copy engine, enqueued on `stream` (a cudaStream_t).  Either end may
+ * be device memory or page-locked host memory; anything else is refused with KG_ERR_INVALID.  Used to
+ * compare the two ways of moving a field to the host. */
+KG_API int kg_diag_copy(void* dst, const void* src, long long bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

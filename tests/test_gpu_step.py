@@ -122,9 +122,9 @@ def test_strip_shape_does_not_change_results(nx, nt, bh):
 
 
 def test_default_strip_shapes():
-    """the library's strip choice: 128 x 16 wherever it gives at least 8000 CTAs, one-warp strips of
-    4 rows for the 2048^2 and 512^2 cases"""
-    for n, want in ((8192, (128, 16)), (4096, (128, 16)), (2048, (32, 4)), (512, (32, 4))):
+    """the library's strip choice: 128 x 32 wherever it gives at least 8000 CTAs (8192^2), else 128 x 16
+    wherever that does (4096^2), one-warp strips of 4 rows for the 2048^2 and 512^2 cases"""
+    for n, want in ((8192, (128, 32)), (4096, (128, 16)), (2048, (32, 4)), (512, (32, 4))):
         sim = Kobayashi(n, n, 1e-4)
         assert sim.tile() == want, (n, sim.tile())
         sim.close()
