@@ -193,11 +193,13 @@ def cpu_baseline_sample(cfg, seconds_budget=20.0):
     return out
 
 
-def measure_ensemble(steps=3000, trial_steps=10):
+def measure_ensemble(steps=3000, trial_steps=10, tune_at=1500):
     """The mixed-size ensemble (512 instances, sides 64..512, per-instance parameters), timed over its
     whole 3000-step workload from the initial state three ways: the autotuned batched form (CUDA graphs
     of 100 steps); the 512 instances as single-grid handles run one after another on one stream (the
-    looped baseline); and the same handles each on its own stream (concurrent single-grid runs)."""
+    looped baseline); and the same handles each on its own stream (concurrent single-grid runs).
+    The autotuner runs on the ensemble's own state at step `tune_at`, the middle of the workload (its
+    trials restore the state they start from), and the timed run starts again from the seeds."""
     import torch
     from crystalgrowth_gb300 import Batch, Kobayashi, configs
     cfg = configs.ensemble_512()
@@ -209,9 +211,11 @@ def measure_ensemble(steps=3000, trial_steps=10):
         for k, i in enumerate(inst):
             b.seed_disks(k, i["disks"])
     seed_batch()
+    b.step(tune_at)
     t0 = time.perf_counter()
     best, _ = b.autotune(trial_steps=trial_steps)
     tune_s = time.perf_counter() - t0
+    seed_batch()
     b.set_tuning(**dict(best, chunk=CHUNK))
     b.step(CHUNK)  # warm-up (graph build)
     seed_batch()
@@ -254,7 +258,7 @@ def measure_ensemble(steps=3000, trial_steps=10):
             "batched_cell_updates_per_s": work / batched_s, "looped_cell_updates_per_s": work / looped_s,
             "concurrent_streams_cell_updates_per_s": work / concurrent_s,
             "speedup_vs_looped": looped_s / batched_s, "speedup_vs_concurrent_streams": concurrent_s / batched_s,
-            "tuning": best, "autotune_s": tune_s,
+            "tuning": best, "autotune_s": tune_s, "tuned_at_step": tune_at,
             "looped": "512 single-grid handles, one after another (each in CUDA graphs of %d steps)" % CHUNK,
             "concurrent_streams": "the same 512 handles, each on its own stream, all enqueued before waiting"}
 

@@ -739,7 +739,7 @@ extern "C" int kg_batch_autotune(kg_batch* b, int trial_steps, kg_batch_tuning* 
         return kg_cuda_fail(e, "kg_batch_autotune setup");
     }
     const int nts[3] = {32, 64, 128};
-    const int bhs[4] = {4, 8, 16, 32};
+    const int bhs[5] = {4, 8, 16, 32, 64};
     /* (mode, streams): one launch per step; the same over 4, 8 or 16 group streams; persistent */
     const int modes[5][2] = {{KG_BATCH_LAUNCH, 1}, {KG_BATCH_LAUNCH, 4}, {KG_BATCH_LAUNCH, 8}, {KG_BATCH_LAUNCH, 16},
                              {KG_BATCH_PERSISTENT, 1}};
@@ -748,7 +748,7 @@ extern "C" int kg_batch_autotune(kg_batch* b, int trial_steps, kg_batch_tuning* 
     for (int kb = 1; kb <= 2 && rc == KG_OK; kb++)
     for (int mi = 0; mi < 5 && rc == KG_OK; mi++)
         for (int ni = 0; ni < 3 && rc == KG_OK; ni++)
-            for (int hi = 0; hi < 4 && rc == KG_OK; hi++) {
+            for (int hi = 0; hi < 5 && rc == KG_OK; hi++) {
                 kg_batch_tuning t{nts[ni], bhs[hi], modes[mi][0], trial_steps, modes[mi][1], kb};
                 rc = kg_batch_set_tuning(b, &t);
                 if (rc)

@@ -49,7 +49,7 @@ KG_API int kg_batch_get_info(const kg_batch* b, int* n, long long* cells, long l
 KG_API int kg_batch_set_tuning(kg_batch* b, const kg_batch_tuning* t);
 KG_API int kg_batch_get_tuning(const kg_batch* b, kg_batch_tuning* t);
 /* Times trial_steps steps of every (nt, bh, mode/streams, tblock) candidate
- * on this batch -- 120 candidates: nt 32/64/128, bh 4/8/16/32, launch mode on
+ * on this batch -- 150 candidates: nt 32/64/128, bh 4/8/16/32/64, launch mode on
  * 1/4/8/16 streams or persistent, 1 or 2 steps per pass -- installs the
  * fastest (keeping the current chunk) and restores the state it started from.
  * best / best_ms_per_step may be NULL. */
