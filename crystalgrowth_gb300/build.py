@@ -81,11 +81,11 @@ def build(force=False, verbose_ptxas=False, quiet=True):
 
 # Compile-time switches of the kernels and the setting each one ships with.  Every other setting
 # computes the same bits (they exist for A/B measurements; the defaults are the measured winners).
-SWITCHES = {"KG_BITS_ASM": 1, "KG_GDIV": 1, "KG_FAR": 1, "KG_FUSE": 1, "KG_QUIET": 3, "KG_IDIV_SUBN": 1,
-            "KG_SLOW_NOINLINE": 1, "KG_TMA": 1}
+SWITCHES = {"KG_BITS_ASM": 1, "KG_GDIV": 1, "KG_FAR": 1, "KG_FUSE": 1, "KG_QUIET": 3, "KG_ABSORB": 1,
+            "KG_IDIV_SUBN": 1, "KG_SLOW_NOINLINE": 1, "KG_TMA": 1}
 # the plain build: every shortcut and every switch in its other setting
-PLAIN = {"KG_BITS_ASM": 0, "KG_GDIV": 0, "KG_FAR": 0, "KG_FUSE": 0, "KG_QUIET": 0, "KG_IDIV_SUBN": 0,
-         "KG_SLOW_NOINLINE": 0, "KG_TMA": 0}
+PLAIN = {"KG_BITS_ASM": 0, "KG_GDIV": 0, "KG_FAR": 0, "KG_FUSE": 0, "KG_QUIET": 0, "KG_ABSORB": 0,
+         "KG_IDIV_SUBN": 0, "KG_SLOW_NOINLINE": 0, "KG_TMA": 0}
 
 
 def build_variant(lib_path, defines):

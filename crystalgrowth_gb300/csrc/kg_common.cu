@@ -221,6 +221,7 @@ int kg_prepare(const kg_params* p, KgDev* d)
     d->m0 = d->a_pi * kg_atan(d->u0);
     d->t_small = kg_absorb_bound(p->teq);
     d->zk = kg_bits(p->K * 0.0);
+    d->ebk = (int)((kg_bits(p->K) >> 52) & 0x7ff);
     /* 1 - phi == 1 needs |phi| <= bound(1) = 2^-55, phi - 0.5 == -0.5 needs bound(0.5) = 2^-56 */
     d->phi_small = kg_absorb_bound(0.5);
     d->r0 = -0.5 + d->m0;

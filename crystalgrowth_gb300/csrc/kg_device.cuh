@@ -60,6 +60,7 @@ struct KgDev {
     double eps0, epsd0, e2_0, ee0; /* eps, eps', eps^2, eps eps' at arg0 */
     double u0, m0;    /* gamma (Teq - 0) and (alpha/pi) atan(u0) */
     uint64_t zk;      /* bits of K * (+0): the T update's latent-heat term for a quiet cell */
+    int ebk;          /* biased exponent field of K (0 for K = 0): bounds the latent-heat term */
     uint64_t t_small; /* |T| bit patterns up to this leave Teq - T == Teq, so u == u0 */
     uint64_t phi_small; /* |phi| bit patterns up to this leave 1 - phi == 1 and phi - 0.5 == -0.5 */
     double r0;          /* -0.5 + m0: the double-well factor (phi - 0.5 + m) of such a cell */
@@ -84,6 +85,12 @@ __device__ __forceinline__ bool kg_neg_big(uint64_t b)
  * 1 as 3, and also settles that cell's eps eps' phi_x, eps eps' phi_y as signed zeros */
 #ifndef KG_QUIET
 #define KG_QUIET 3
+#endif
+
+/* 1: the latent-heat term K (phi' - phi) of the T update is skipped where a bound on exponents shows
+ * that rounding absorbs it (exact); 0: always computed */
+#ifndef KG_ABSORB
+#define KG_ABSORB 1
 #endif
 
 /* 1: the angle's quotient gy/gx through kg_gdiv (the IEEE bits on the integer pipes); 0: the
@@ -269,8 +276,28 @@ __device__ __forceinline__ void kg_stage2(const KgDev& P, double e2c, double gx,
 #endif
         react = old_phi * (1.0 - old_phi) * (old_phi - 0.5 + m);
     double rhs = acc + react;
-    double new_phi = old_phi + kg_idiv(rhs * P.dt, &P.itau);
+    const double q = kg_idiv(rhs * P.dt, &P.itau);
+    double new_phi = old_phi + q;
+#if KG_ABSORB
+    /* The reference's T' = (T + lap_T dt) + K (phi' - phi) = x + y.  With eb the biased exponent field
+     * (|v| < 2^(eb - 1022) for every finite v): phi' - phi = q + e, |e| <= ulp(phi')/2 <=
+     * 2^(max(eb_phi', 1) - 1076), so |d| = |RN(phi' - phi)| <= 2^(M + 1) with
+     * M = max(eb_q - 1022, max(eb_phi', 1) - 1076), and |y| = |RN(K d)| <= 2^(eb_K - 1021 + M).  For a
+     * normal x (2^(eb_x - 1023) <= |x|), eb_K + M + 56 < eb_x gives |y| < 2^(eb_x - 1077) = ulp(x)/4, so
+     * RN(x + y) = x (a tie below a power of two rounds to x, whose significand is even).  Non-finite
+     * q or phi' (eb = 2047) and zero, subnormal or non-finite x take the full expression. */
+    const double x = old_t + lap_t * P.dt;
+    const int ebx = (int)((kg_bits(x) >> 52) & 0x7ff);
+    const int ebq = (int)((kg_bits(q) >> 52) & 0x7ff);
+    const int ebn = max((int)((kg_bits(new_phi) >> 52) & 0x7ff), 1);
+    const int M = max(ebq - 1022, ebn - 1076);
+    if (ebx >= 1 && ebx <= 2046 && P.ebk + M + 56 < ebx)
+        t = x;
+    else
+        t = x + P.K * (new_phi - old_phi);
+#else
     t = old_t + lap_t * P.dt + P.K * (new_phi - old_phi);
+#endif
     phi = new_phi;
     if (aux) {
         aux->rhs = rhs;

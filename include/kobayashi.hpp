@@ -92,6 +92,15 @@ class Kobayashi {
             throw Error(KG_ERR_INVALID, "setFields: size mismatch");
         check(kg_set_fields(h_, phi.data(), t.data(), th.data()));
     }
+    /* strip shape and temporal blocking (kg_set_tile, kg_set_tblock): speed only, the same bits */
+    void setTile(int nt, int bh) { check(kg_set_tile(h_, nt, bh)); }
+    void setTblock(int k) { check(kg_set_tblock(h_, k)); }
+    int tblock() const
+    {
+        int k = 1;
+        check(kg_get_tblock(h_, &k));
+        return k;
+    }
     long long steps() const
     {
         long long s = 0, f = 0;

@@ -40,6 +40,16 @@ int main()
             caught = e.code == KG_ERR_INVALID;
         }
         std::printf("invalid params rejected %d\n", caught ? 1 : 0);
+        // the same 30 frames with two time steps per pass: the same bits
+        kg::Kobayashi sim2(250, 250, 0.0001);
+        sim2.setTblock(2);
+        for (int frame = 0; frame < 30; frame++)
+            sim2.iUpdate();
+        uint64_t h2 = 1469598103934665603ull;
+        h2 = fnv(sim2.phi(), h2);
+        h2 = fnv(sim2.T(), h2);
+        h2 = fnv(sim2.theta(), h2);
+        std::printf("tblock %d same %d\n", sim2.tblock(), h2 == h ? 1 : 0);
     } catch (const kg::Error& e) {
         std::printf("error %d %s\n", e.code, e.what());
         return 1;

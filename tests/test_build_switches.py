@@ -13,7 +13,7 @@ import pytest
 
 from crystalgrowth_gb300 import build as kbuild
 
-SETTINGS = {"KG_BITS_ASM": [0], "KG_GDIV": [0], "KG_FAR": [0], "KG_FUSE": [0], "KG_QUIET": [0, 1, 2],
+SETTINGS = {"KG_BITS_ASM": [0], "KG_GDIV": [0], "KG_FAR": [0], "KG_FUSE": [0], "KG_QUIET": [0, 1, 2], "KG_ABSORB": [0],
             "KG_IDIV_SUBN": [0], "KG_SLOW_NOINLINE": [0], "KG_TMA": [0]}
 
 

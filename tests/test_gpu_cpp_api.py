@@ -43,3 +43,4 @@ def test_cpp_class_runs_like_the_reference_main(tmp_path):
     sim.close()
     assert out[1] == "reset 0 0"
     assert out[2] == "invalid params rejected 1"
+    assert out[3] == "tblock 2 same 1"
