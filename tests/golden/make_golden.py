@@ -158,11 +158,36 @@ def field_hashes(phi, t, th):
     return dict(sha_phi=sha(phi), sha_T=sha(t), sha_theta=sha(th))
 
 
+def _variants_done(path):
+    try:
+        return json.load(open(path)).get("variants_2048", {}).get("variants", {})
+    except (OSError, ValueError):
+        return {}
+
+
 def _variant_job(args):
-    v, threads = args
+    v, threads, path = args
+    if v["name"] in _variants_done(path):  # another process finished it meanwhile
+        return v["name"], None
     st = ko_oracle.port_run(*configs.initial_fields(v["nx"], v["ny"], v["disks"]), v["params"], v["steps"],
                             libm=False, threads=threads)
     return v["name"], field_hashes(*st)
+
+
+def _merge_variants(path, steps, found):
+    """adds `found` to the variants in `path` under a file lock (several processes may share the file)
+    and returns everything the file then holds"""
+    import fcntl
+    with open(path + ".lock", "w") as lk:
+        fcntl.flock(lk, fcntl.LOCK_EX)
+        doc = json.load(open(path)) if os.path.exists(path) else {}
+        vd = doc.setdefault("variants_2048", {"steps": steps, "variants": {}})
+        vd["variants"].update(found)
+        tmp = path + ".tmp%d" % os.getpid()
+        with open(tmp, "w") as f:
+            json.dump(doc, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+        return dict(vd["variants"])
 
 
 def _instance_job(args):
@@ -214,14 +239,21 @@ def write_full_configs():
                 _save_full(doc)
                 print("grid_8192 step %d at %.0f s" % (m, time.time() - t0), flush=True)
     if part in ("all", "variants"):
+        # written to `--out` (default: the fixture itself) with locked merges, so that several processes
+        # can share the list: each skips the variants already present
+        out = _arg("--out", FULL)
         vs = configs.variants_2048()
-        vd = doc.setdefault("variants_2048", {"steps": vs[0]["steps"], "variants": {}})
-        todo = [(v, 1) for v in vs if v["name"] not in vd["variants"]]
+        if "--reverse" in sys.argv[1:]:
+            vs = vs[::-1]
+        found = dict(doc.get("variants_2048", {}).get("variants", {})) if out == FULL else {}
+        found.update(_variants_done(out))
+        todo = [(v, 1, out) for v in vs if v["name"] not in found]
         t0 = time.time()
         with cf.ProcessPoolExecutor(max_workers=threads, mp_context=ctx) as ex:
             for name, h in ex.map(_variant_job, todo):
-                vd["variants"][name] = h
-                _save_full(doc)
+                if h is None:
+                    continue
+                _merge_variants(out, vs[0]["steps"], {name: h})
                 print("variant %s at %.0f s" % (name, time.time() - t0), flush=True)
 
 

@@ -22,13 +22,21 @@ from crystalgrowth_gb300 import Batch, Kobayashi, configs
 from crystalgrowth_gb300.batch import KG_BATCH_LAUNCH, KG_BATCH_PERSISTENT
 
 pytestmark = pytest.mark.gpu
-FULL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "full_configs.json")
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FULL = os.path.join(GOLD, "full_configs.json")
+# variants computed by a second oracle process, merged into FULL once complete
+VARIANTS = os.path.join(GOLD, "full_configs_variants.json")
 
 
 def load():
     if not os.path.exists(FULL):
         pytest.skip("no full-length fixture")
-    return json.load(open(FULL))
+    doc = json.load(open(FULL))
+    if os.path.exists(VARIANTS):
+        more = json.load(open(VARIANTS)).get("variants_2048", {})
+        vd = doc.setdefault("variants_2048", {"steps": more.get("steps", 5000), "variants": {}})
+        vd["variants"].update(more.get("variants", {}))
+    return doc
 
 
 def sha(a):
@@ -57,15 +65,15 @@ def test_grid8192_full_trajectory():
     sim.close()
 
 
-VARIANTS = {v["name"]: v for v in configs.variants_2048()}
+VARIANT_CFG = {v["name"]: v for v in configs.variants_2048()}
 
 
-@pytest.mark.parametrize("name", sorted(VARIANTS))
+@pytest.mark.parametrize("name", sorted(VARIANT_CFG))
 def test_variant_2048_full_length(name):
     vd = load().get("variants_2048", {}).get("variants", {})
     if name not in vd:
         pytest.skip("variant not in the fixture yet")
-    v = VARIANTS[name]
+    v = VARIANT_CFG[name]
     sim = Kobayashi(v["nx"], v["ny"], v["params"]["dt"], params=v["params"])
     sim.seed_disks(v["disks"])
     sim.step(v["steps"])
