@@ -110,6 +110,7 @@ _SIGS = {
     "kg_diag_fp64_probe": [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                            ctypes.POINTER(ctypes.c_double)],
     "kg_diag_inject_timeout": [_vp],
+    "kg_diag_batch_inject_timeout": [_vp],
     "kg_diag_copy": [_vp, _vp, ctypes.c_longlong, _vp],
 }
 _RESTYPE = {"kg_last_error": ctypes.c_char_p, "kg_version": ctypes.c_char_p}

@@ -415,6 +415,17 @@ static int batch_check_barrier(kg_batch* b)
     return KG_OK;
 }
 
+/* Host-side fault injection for tests: raises the grid barrier's error flag as a CTA whose bounded wait
+ * ran out would, and reads it back as kg_batch_step does after a persistent chunk (no kernel runs). */
+extern "C" int kg_diag_batch_inject_timeout(kg_batch* b)
+{
+    if (!b)
+        return kg_fail(KG_ERR_INVALID, "null kg_batch handle");
+    KgBarrier h{0, 0, 1, 0};
+    KG_CUDA(cudaMemcpyAsync(b->d_bar, &h, sizeof h, cudaMemcpyHostToDevice, b->stream));
+    return batch_check_barrier(b);
+}
+
 /* instance k's state was replaced: the time-out latch clears once every instance's has been */
 static void batch_replaced(kg_batch* b, int k)
 {

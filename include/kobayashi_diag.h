@@ -42,6 +42,12 @@ KG_API int kg_diag_mbar_timeout(int* timed_out);
  * KG_ERR_TIMEOUT, and kg_step then refuses until the state is replaced. */
 KG_API int kg_diag_inject_timeout(kg_sim* h);
 
+/* The same for a batch: raises the grid barrier's error flag as a persistent CTA whose wait ran out
+ * does, and reads it back as kg_batch_step does (returns KG_ERR_TIMEOUT).  kg_batch_step then refuses
+ * until every instance's state has been replaced. */
+struct kg_batch;
+KG_API int kg_diag_batch_inject_timeout(struct kg_batch* b);
+
 /* FP64 pipe probe on the current device: every thread runs `chains` (4, 8 or
  * 16) independent dependency chains of one FP64 operation -- op 0: FMA,
  * 1: add, 2: multiply, 3: two adds per multiply -- in ctas_per_sm CTAs of

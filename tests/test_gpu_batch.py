@@ -161,3 +161,28 @@ def test_batch_group_streams_bitwise(streams, chunk):
         for x, y in zip(b.fields(k), ref[k]):
             assert bits_equal(x, y), k
     b.close()
+
+
+def test_batch_timeout_latch():
+    """after a grid-barrier wait ran out (injected on the host), kg_batch_step refuses until every
+    instance's state has been replaced; then the batch steps on, bit-identical to the oracle"""
+    inst = small_ensemble(count=3, seed=5, lo=20, hi=60)
+    b = make_batch(inst)
+    b.step(4)
+    rc = _lib.lib().kg_diag_batch_inject_timeout(b._h)
+    assert rc == _lib.KG_ERR_TIMEOUT
+    with pytest.raises(_lib.KgError) as e:
+        b.step(1)
+    assert e.value.code == _lib.KG_ERR_TIMEOUT
+    b.seed_disks(0, inst[0]["disks"])
+    b.seed_disks(1, inst[1]["disks"])
+    with pytest.raises(_lib.KgError):
+        b.step(1)  # instance 2 still holds the unreliable state
+    init = configs.initial_fields(inst[2]["nx"], inst[2]["ny"], inst[2]["disks"])
+    b.set_fields(2, *init)
+    b.step(9)
+    ref = oracle(inst, 9)
+    for k in range(len(inst)):
+        for x, y in zip(b.fields(k), ref[k]):
+            assert bits_equal(x, y)
+    b.close()
