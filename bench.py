@@ -325,8 +325,12 @@ def run_reference(args, rank, world):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "grid_8192: 8192x8192 FP64 Kobayashi step, 64 seeded disks r=4..8",
-                       "bench_step": "1 time step on the host (reference CPU path)", "disks_seed": 8192},
+            "config": {"workload": "grid_%d: %dx%d FP64 Kobayashi step, %d seeded disks r=4..8, "
+                                   "delta=0.02 theta0=0.2" % (nx, nx, ny, len(cfg["disks"])),
+                       "bench_step": "1 time step on the host (reference CPU path)", "disks_seed": 8192,
+                       "l2": "inputs larger than L2 (3.2 GB state)",
+                       "note": "the reference's model has no theta0: it steps the same state with theta0 = 0 "
+                               "(the cost per cell does not depend on theta0)"},
             "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": 1, "kind": kind,
                              "sample": "%d timed time steps of the 8192^2 state, single thread" % args.steps},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
