@@ -22,21 +22,13 @@ from crystalgrowth_gb300 import Batch, Kobayashi, configs
 from crystalgrowth_gb300.batch import KG_BATCH_LAUNCH, KG_BATCH_PERSISTENT
 
 pytestmark = pytest.mark.gpu
-GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FULL = os.path.join(GOLD, "full_configs.json")
-# variants computed by a second oracle process, merged into FULL once complete
-VARIANTS = os.path.join(GOLD, "full_configs_variants.json")
+FULL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "full_configs.json")
 
 
 def load():
     if not os.path.exists(FULL):
         pytest.skip("no full-length fixture")
-    doc = json.load(open(FULL))
-    if os.path.exists(VARIANTS):
-        more = json.load(open(VARIANTS)).get("variants_2048", {})
-        vd = doc.setdefault("variants_2048", {"steps": more.get("steps", 5000), "variants": {}})
-        vd["variants"].update(more.get("variants", {}))
-    return doc
+    return json.load(open(FULL))
 
 
 def sha(a):
