@@ -38,7 +38,10 @@
  *     signed zero, so phi stays +0 and only T + lap_T dt is computed; with a
  *     +0 T neighbourhood as well, T stays +0 too.  Stage 1 of a cell whose
  *     four phi neighbours are +0 keeps theta and takes gx = gy = +0 without
- *     arithmetic.
+ *     arithmetic;
+ *   - the T update's latent-heat term K (phi' - phi) is not computed where
+ *     a bound on the operands' exponents shows that adding it to
+ *     T + lap_T dt cannot change the sum (kg_stage2).
  * Comparisons use the bit patterns (integer pipe), never the FP64 pipe: kg_bits
  * takes them through an inline-PTX move, so the optimiser cannot turn a bit
  * test back into an FP64 comparison.  atan, sin and cos (kg_math.h) run on
