@@ -361,9 +361,16 @@ def run_ours(args, rank, world):
     # steps 0 .. 100 K of the workload's trajectory (K = 100: the whole 10,000-step run)
     for _ in range(args.warmup):
         sim.step(CHUNK)
-    sim.seed_disks(cfg["disks"])
-    if args.skip_to:
-        sim.step(args.skip_to)  # untimed: the timed window starts later in the trajectory
+    start = args.skip_to
+    if args.load_snapshot:
+        sim.load(args.load_snapshot)  # the timed window starts at the snapshot's step
+        start = sim.counters()[0]
+    else:
+        sim.seed_disks(cfg["disks"])
+        if args.skip_to:
+            sim.step(args.skip_to)  # untimed: the timed window starts later in the trajectory
+    if args.save_snapshot:
+        sim.save(args.save_snapshot)
     sim.sync()
 
     # one event at every chunk boundary: the whole timed run, and the time of each 100-step chunk
@@ -436,7 +443,7 @@ def run_ours(args, rank, world):
     pts = []
     pk = None
     for step, opc in sorted((int(k), float(v)) for k, v in samples.items()):
-        k = (step - args.skip_to) // CHUNK
+        k = (step - start) // CHUNK
         if 0 <= k < len(chunk_ms):
             if pk is None:
                 pk, per_clk = fp64_peak()
@@ -464,7 +471,7 @@ def run_ours(args, rank, world):
                                    "delta=0.02 theta0=0.2" % (nx, nx, ny, args.disks),
                        "bench_step": "one CUDA graph of %d time steps" % CHUNK,
                        "steps_timed": "time steps %d..%d of the trajectory from the seeded state (the "
-                                      "workload is 10,000 steps)" % (args.skip_to, args.skip_to + args.steps * CHUNK),
+                                      "workload is 10,000 steps)" % (start, start + args.steps * CHUNK),
                        "e2e_steps": "%d chunks continuing from the timed run's final state, after one untimed "
                                     "round trip" % e2e_steps,
                        "strips": "%d threads x %d rows" % sim.tile(),
@@ -507,6 +514,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (short profiling runs)")
     ap.add_argument("--skip-to", type=int, default=0,
                     help="advance this many time steps untimed before the timed window (profiling of later windows)")
+    ap.add_argument("--save-snapshot", default="", help="write the state at the start of the timed window to this "
+                    "file (kg_save), for profiling a later window without replaying the trajectory")
+    ap.add_argument("--load-snapshot", default="", help="start the timed window from this snapshot (kg_load) "
+                    "instead of the seeds")
     ap.add_argument("--tblock", type=int, default=1, help="time steps per pass over HBM (1, or 2: temporal blocking)")
     args = ap.parse_args()
     rank, world = dist_init(args.gpus)
