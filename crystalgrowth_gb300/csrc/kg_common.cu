@@ -228,23 +228,26 @@ int kg_prepare(const kg_params* p, KgDev* d)
     return KG_OK;
 }
 
-/* Strip shape for one grid.  Strips of 128 x 32 wherever they still give at
- * least 8,000 CTAs (8192^2 and up), else 128 x 16 wherever that gives 8,000
- * (4096^2).  Measured on GB300 at 8192^2: 128 x 32 ran 0.4% faster than
- * 128 x 16 over time steps 0-1000 and 2.5% faster over steps 8000-9000 (fewer
- * halo rows recomputed); at 4096^2 late in the trajectory 128 x 16 beat
- * 128 x 32 (1.01e10 against 9.7e9).  Smaller grids: the largest strips that
- * still give about 30,000 CTAs (below that, strips covering the growing
- * crystals finish last and the SMs idle; above it, the repeated halo rows of
- * short strips cost more than they save), down to one-warp strips of 4 rows. */
+/* Strip shape for one grid.  The first of 256 x 24, 128 x 32 and 128 x 16 that still gives at least
+ * 8,000 CTAs (256 x 24 for 8192^2 and up, 128 x 16 for 4096^2).  Measured on GB300 at 8192^2
+ * (cell-updates/s over steps 0-1000 / 4000-5000 / 8000-9000): 256 x 24 2.497e10 / 1.175e10 / 9.875e9,
+ * 128 x 32 2.497e10 / 1.137e10 / 9.517e9, 128 x 16 2.485e10 / - / 9.279e9: wider and taller strips
+ * recompute fewer halo columns and rows, and half as many CTAs start.  At 4096^2 late in the
+ * trajectory 128 x 16 beat 128 x 32 (1.01e10 against 9.7e9).  Smaller grids: the largest strips that
+ * still give about 30,000 CTAs (below that, strips covering the growing crystals finish last and the
+ * SMs idle; above it, the repeated halo rows of short strips cost more than they save), down to
+ * one-warp strips of 4 rows. */
 void kg_pick_tile(int nx, int ny, int* nt, int* bh)
 {
-    for (int h : {32, 16})
-        if ((long long)((nx + 125) / 126) * ((ny + h - 1) / h) >= 8000) {
-            *nt = 128;
+    const int big[3][2] = {{256, 24}, {128, 32}, {128, 16}};
+    for (int k = 0; k < 3; k++) {
+        const int t = big[k][0], h = big[k][1];
+        if ((long long)((nx + t - 3) / (t - 2)) * ((ny + h - 1) / h) >= 8000) {
+            *nt = t;
             *bh = h < ny ? h : ny;
             return;
         }
+    }
     const long long want = 30000;
     const int shapes[8][2] = {{128, 64}, {128, 32}, {128, 16}, {64, 16}, {64, 8}, {32, 8}, {32, 4}};
     for (int k = 0; k < 7; k++) {

@@ -92,11 +92,13 @@ static int launch_step(kg_sim* h, int from, int k = 1)
     double* const* a = h->buf[from];
     double* const* b = h->buf[from ^ 1];
     if (k == 2) {
-        dim3 grid((h->nx + h->nt - 7) / (h->nt - 6), (h->ny + h->bh - 1) / h->bh);
-        if (h->nt == 32)
+        /* the two-step pass holds two pipelines' rings: strips of at most 128 threads */
+        const int nt2 = h->nt > 128 ? 128 : h->nt;
+        dim3 grid((h->nx + nt2 - 7) / (nt2 - 6), (h->ny + h->bh - 1) / h->bh);
+        if (nt2 == 32)
             kg_step2_kernel<32><<<grid, 32, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1],
                                                              b[2]);
-        else if (h->nt == 64)
+        else if (nt2 == 64)
             kg_step2_kernel<64><<<grid, 64, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1],
                                                              b[2]);
         else
@@ -110,6 +112,9 @@ static int launch_step(kg_sim* h, int from, int k = 1)
         else if (h->nt == 64)
             kg_step_kernel<64><<<grid, 64, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0], b[1],
                                                             b[2], h->err);
+        else if (h->nt == 256)
+            kg_step_kernel<256><<<grid, 256, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0],
+                                                              b[1], b[2], h->err);
         else
             kg_step_kernel<128><<<grid, 128, 0, h->stream>>>(h->dev, h->nx, h->ny, h->bh, a[0], a[1], a[2], b[0],
                                                               b[1], b[2], h->err);
@@ -299,8 +304,8 @@ extern "C" int kg_set_tile(kg_sim* h, int nt, int bh)
     int rc = check(h);
     if (rc)
         return rc;
-    if (nt != 32 && nt != 64 && nt != 128)
-        return kg_fail(KG_ERR_INVALID, "kg_set_tile: nt must be 32, 64 or 128");
+    if (nt != 32 && nt != 64 && nt != 128 && nt != 256)
+        return kg_fail(KG_ERR_INVALID, "kg_set_tile: nt must be 32, 64, 128 or 256");
     if (bh < 1 || bh > 65536)
         return kg_fail(KG_ERR_INVALID, "kg_set_tile: bh must lie in [1, 65536]");
     KG_CUDA(cudaStreamSynchronize(h->stream));

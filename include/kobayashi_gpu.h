@@ -144,10 +144,11 @@ KG_API int kg_get_stream(kg_sim* h, void** stream);
 KG_API int kg_step_noalloc(int nx, int ny, const kg_params* p, double* phi, double* T, double* theta,
                            long long nsteps, void* stream);
 
-/* Strip shape of the fused step: nt threads per CTA (32, 64 or 128; the strip
- * is nt - 2 columns wide) and bh rows per strip.  kg_create picks the largest
- * strips that still give the GPU about 30,000 CTAs; results do not depend on
- * the shape. */
+/* Strip shape of the fused step: nt threads per CTA (32, 64, 128 or 256; the
+ * strip is nt - 2 columns wide) and bh rows per strip.  kg_create picks 256 x 24,
+ * 128 x 32 or 128 x 16 where that still gives at least 8,000 CTAs, else the
+ * largest strips that give about 30,000.  Results do not depend on the shape;
+ * two steps per pass (kg_set_tblock) use strips of at most 128 threads. */
 KG_API int kg_set_tile(kg_sim* h, int nt, int bh);
 KG_API int kg_get_tile(const kg_sim* h, int* nt, int* bh);
 

@@ -103,7 +103,8 @@ def test_graph_chunks_do_not_change_results():
 
 
 @pytest.mark.parametrize("nx", [141, 260])
-@pytest.mark.parametrize("nt,bh", [(32, 1), (32, 17), (64, 1), (64, 8), (64, 40), (128, 3), (128, 16), (128, 200)])
+@pytest.mark.parametrize("nt,bh", [(32, 1), (32, 17), (64, 1), (64, 8), (64, 40), (128, 3), (128, 16), (128, 200),
+                                   (256, 1), (256, 24), (256, 200)])
 def test_strip_shape_does_not_change_results(nx, nt, bh):
     """odd width: every strip loads its columns lane by lane; even width (260): interior strips
     stage their rows with bulk copies, across strip heights that wrap each 8-row ring several times"""
@@ -122,9 +123,9 @@ def test_strip_shape_does_not_change_results(nx, nt, bh):
 
 
 def test_default_strip_shapes():
-    """the library's strip choice: 128 x 32 wherever it gives at least 8000 CTAs (8192^2), else 128 x 16
-    wherever that does (4096^2), one-warp strips of 4 rows for the 2048^2 and 512^2 cases"""
-    for n, want in ((8192, (128, 32)), (4096, (128, 16)), (2048, (32, 4)), (512, (32, 4))):
+    """the library's strip choice: the first of 256 x 24, 128 x 32, 128 x 16 that gives at least 8000
+    CTAs (8192^2: 256 x 24; 4096^2: 128 x 16), one-warp strips of 4 rows for the 2048^2 and 512^2 cases"""
+    for n, want in ((8192, (256, 24)), (4096, (128, 16)), (2048, (32, 4)), (512, (32, 4))):
         sim = Kobayashi(n, n, 1e-4)
         assert sim.tile() == want, (n, sim.tile())
         sim.close()

@@ -52,8 +52,9 @@ def test_k2_bitwise_small_and_ragged(nx, ny, steps):
         assert bits_equal(x, y)
 
 
-@pytest.mark.parametrize("nt,bh", [(32, 1), (32, 5), (64, 2), (64, 33), (128, 4), (128, 16), (128, 200)])
+@pytest.mark.parametrize("nt,bh", [(32, 1), (32, 5), (64, 2), (64, 33), (128, 4), (128, 16), (128, 200), (256, 24)])
 def test_k2_strip_shapes(nt, bh):
+    """(256-thread strips: the two-step pass runs on 128-thread strips of the same height)"""
     p = dict(configs.BASE, delta=0.05, theta0=0.7)
     disks = [(70, 50, 6), (10, 90, 4), (120, 30, 5)]
     a = run_k2(141, 103, p, disks, 90, tile=(nt, bh))
