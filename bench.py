@@ -361,14 +361,18 @@ def run_ours(args, rank, world):
     # steps 0 .. 100 K of the workload's trajectory (K = 100: the whole 10,000-step run)
     for _ in range(args.warmup):
         sim.step(CHUNK)
-    start = args.skip_to
-    if args.load_snapshot:
-        sim.load(args.load_snapshot)  # the timed window starts at the snapshot's step
-        start = sim.counters()[0]
-    else:
+
+    def to_window_start():
+        """the state at the first time step of the timed window; returns that step"""
+        if args.load_snapshot:
+            sim.load(args.load_snapshot)  # the timed window starts at the snapshot's step
+            return sim.counters()[0]
         sim.seed_disks(cfg["disks"])
         if args.skip_to:
             sim.step(args.skip_to)  # untimed: the timed window starts later in the trajectory
+        return args.skip_to
+
+    start = to_window_start()
     if args.save_snapshot:
         sim.save(args.save_snapshot)
     sim.sync()
@@ -394,18 +398,21 @@ def run_ours(args, rank, world):
     value = world * cells * CHUNK * args.steps / (ms / 1e3)
     launch_s = ms_per_step / 1e3 / CHUNK  # average duration of one step-kernel launch
 
-    # end to end through the C ABI with host buffers: upload state, 100 steps, download state
-    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 3))
+    # end to end through the C ABI with host buffers, over the same time-step window as the timed run:
+    # every chunk uploads the state, takes 100 steps and downloads the state
+    e2e_steps = 0 if args.no_e2e else args.steps
     e2e_value = None
     e2e_parts = None
     if e2e_steps:
         pinned = [torch.empty((ny, nx), dtype=torch.float64, pin_memory=True) for _ in range(3)]
         host = [t.numpy() for t in pinned]
-        # filled by a download, not by the CPU, then one untimed round trip: the first device write
-        # into host lines the CPU holds dirty runs at a fraction of the link's speed
+        final = [t.numpy() for t in (torch.empty((ny, nx), dtype=torch.float64, pin_memory=True) for _ in range(3))]
+        sim.fields(out=final)  # the timed run's final state
+        # the buffers are filled by a download, not by the CPU, then one untimed round trip: the first
+        # device write into host lines the CPU holds dirty runs at a fraction of the link's speed
+        to_window_start()
         sim.fields(out=host)
         sim.set_fields(*host)
-        sim.step(CHUNK)
         sim.fields(out=host)
         barrier(world)
         torch.cuda.synchronize()
@@ -430,7 +437,10 @@ def run_ours(args, rank, world):
         e2e_parts = {"upload_ms": 1e3 * parts[0] / e2e_steps, "steps_ms": 1e3 * parts[1] / e2e_steps,
                      "download_ms": 1e3 * parts[2] / e2e_steps,
                      "upload_gbs": state_bytes * e2e_steps / parts[0] / 1e9,
-                     "download_gbs": state_bytes * e2e_steps / parts[2] / 1e9}
+                     "download_gbs": state_bytes * e2e_steps / parts[2] / 1e9,
+                     "same_final_state": all(np.array_equal(a.view(np.uint64), b.view(np.uint64))
+                                             for a, b in zip(host, final))}
+        del pinned, host, final
 
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_CELL * cells / launch_s / 1e9
@@ -472,8 +482,9 @@ def run_ours(args, rank, world):
                        "bench_step": "one CUDA graph of %d time steps" % CHUNK,
                        "steps_timed": "time steps %d..%d of the trajectory from the seeded state (the "
                                       "workload is 10,000 steps)" % (start, start + args.steps * CHUNK),
-                       "e2e_steps": "%d chunks continuing from the timed run's final state, after one untimed "
-                                    "round trip" % e2e_steps,
+                       "e2e_steps": "the timed window again (%d chunks from time step %d), after one untimed "
+                                    "round trip; same_final_state: its downloaded final state equals the timed "
+                                    "run's, bit for bit" % (e2e_steps, start),
                        "strips": "%d threads x %d rows" % sim.tile(),
                        "tblock": sim.tblock(),
                        "l2": "inputs larger than L2 (3.2 GB state)", "parallelism": "replicas" if world > 1 else "1 GPU"},
