@@ -263,6 +263,54 @@ def measure_ensemble(steps=3000, trial_steps=10, tune_at=1500):
             "concurrent_streams": "the same 512 handles, each on its own stream, all enqueued before waiting"}
 
 
+def ensemble_window(args):
+    """The batched ensemble's step time at one point of its trajectory, with one launch-mode tuning (no
+    autotuning): the state comes from the seeds advanced --ensemble-at steps, or from a file written
+    by --ensemble-save; W warm-up steps, then K timed steps (CUDA events).  For profiling the batched
+    kernel at a later state without replaying the trajectory under a profiler."""
+    import numpy as np
+    import torch
+    from crystalgrowth_gb300 import Batch, configs
+    inst = configs.ensemble_512()["instances"]
+    cells = sum(i["nx"] * i["ny"] for i in inst)
+    b = Batch([(i["nx"], i["ny"]) for i in inst], [i["params"] for i in inst])
+    if args.ensemble_load:
+        snap = np.load(args.ensemble_load)
+        start, flat = int(snap["step"]), snap["state"]
+        off = 0
+        for k, i in enumerate(inst):
+            n = i["nx"] * i["ny"]
+            b.set_fields(k, flat[off:off + n], flat[off + n:off + 2 * n], flat[off + 2 * n:off + 3 * n])
+            off += 3 * n
+    else:
+        start = args.ensemble_at
+        for k, i in enumerate(inst):
+            b.seed_disks(k, i["disks"])
+        b.set_tuning(nt=64, bh=64, mode=0, chunk=CHUNK, streams=4, tblock=1)
+        b.step(start)
+    if args.ensemble_save:
+        b.sync()
+        np.savez(args.ensemble_save, step=start,
+                 state=np.concatenate([a.ravel() for k in range(len(inst)) for a in b.fields(k)]))
+    nt, bh, streams = (int(v) for v in args.ensemble_tuning.split(","))
+    b.set_tuning(nt=nt, bh=bh, mode=0, chunk=max(1, min(args.steps, CHUNK)), streams=streams, tblock=1)
+    stream = torch.cuda.ExternalStream(b.stream())
+    b.step(args.warmup)
+    b.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    b.close()
+    print(json.dumps({"ensemble_window": "ensemble_512, time steps %d..%d" % (start + args.warmup,
+                                                                             start + args.warmup + args.steps),
+                      "ms_per_step": ms, "cell_updates_per_s": cells / ms * 1e3,
+                      "tuning": {"nt": nt, "bh": bh, "mode": 0, "streams": streams, "tblock": 1}}), flush=True)
+    return 0
+
+
 def measure_adjoint():
     """Adjoint/forward cost on the 512^2, 4000-step rollout with checkpoints every 64 steps."""
     import numpy as np
@@ -530,7 +578,15 @@ def main():
     ap.add_argument("--load-snapshot", default="", help="start the timed window from this snapshot (kg_load) "
                     "instead of the seeds")
     ap.add_argument("--tblock", type=int, default=1, help="time steps per pass over HBM (1, or 2: temporal blocking)")
+    ap.add_argument("--ensemble-at", type=int, default=-1, help="time only the batched ensemble, K steps after "
+                    "W warm-up steps from this time step (profiling of the batched kernel)")
+    ap.add_argument("--ensemble-save", default="", help="with --ensemble-at: write the state at that step here (.npz)")
+    ap.add_argument("--ensemble-load", default="", help="time only the batched ensemble, from a state written by "
+                    "--ensemble-save")
+    ap.add_argument("--ensemble-tuning", default="64,64,1", help="NT,BH,STREAMS of the ensemble window (launch mode)")
     args = ap.parse_args()
+    if args.ensemble_at >= 0 or args.ensemble_load:
+        return ensemble_window(args)
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":
         return run_reference(args, rank, world)
