@@ -122,6 +122,24 @@ def test_strip_shape_does_not_change_results(nx, nt, bh):
         assert bits_equal(x, y)
 
 
+@pytest.mark.parametrize("nt,nx", [(256, 2), (256, 3), (256, 254), (256, 255), (256, 256), (256, 510), (256, 512),
+                                   (256, 766), (128, 126), (128, 252), (128, 254), (128, 380)])
+def test_strip_edges_against_grid_width(nt, nx):
+    """widths around the bulk-copy condition (an even width and a strip lying inside the grid: i0 >= 2,
+    i0 + NT <= nx) and single strips that wrap a grid narrower than themselves"""
+    p = dict(configs.BASE)
+    disks = [(nx // 2, 18, 5), (nx // 5, 30, 3)]
+    sim = Kobayashi(nx, 37, p["dt"], params=p)
+    sim.seed_disks(disks)
+    sim.set_tile(nt, 7)
+    sim.step(40)
+    a = sim.fields()
+    sim.close()
+    b = oracle_run(nx, 37, p, disks, 40)
+    for x, y in zip(a, b):
+        assert bits_equal(x, y)
+
+
 def test_default_strip_shapes():
     """the library's strip choice: the first of 256 x 24, 128 x 32, 128 x 16 that gives at least 8000
     CTAs (8192^2: 256 x 24; 4096^2: 128 x 16), one-warp strips of 4 rows for the 2048^2 and 512^2 cases"""
